@@ -1,0 +1,375 @@
+// CTMRG on the device: ctmrgstep (src/ctmrg.jl:126-153), its pullback, the
+// fixed-point loop with the StopFunction semantics of src/fixedpoint.jl:17-41,
+// and the reverse pass over a recorded run (the Zygote gradient of the
+// unrolled loop).  All tensors are column-major, in the reference's index order:
+//   bulk a: d×d×d×d,  corner C: χ×χ,  edge T: χ×d×χ,  n = χd.
+#include <cmath>
+#include <limits>
+
+#include "tnad_drivers.h"
+
+namespace tnad {
+
+double* DevPool::d(int64_t n) {
+  void* p = nullptr;
+  size_t bytes = (size_t)std::max<int64_t>(n, 1) * 8;
+  cudaError_t e = cudaMalloc(&p, bytes);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    fail(TNAD_ERR_NOMEM, "tape cudaMalloc failed");
+  }
+  ptrs.push_back(p);
+  this->bytes += (int64_t)bytes;
+  return (double*)p;
+}
+
+void DevPool::free_all() {
+  for (void* p : ptrs) cudaFree(p);
+  ptrs.clear();
+  bytes = 0;
+}
+
+__global__ void k_init_raw(const double* __restrict__ a, int d, int chi, double* __restrict__ C,
+                           double* __restrict__ T) {
+  // C[i,j] = Σ_kl a[i,j,k,l] for i,j < min(d,χ), else 0 ; T[i,j,k] = Σ_l a[i,j,k,l]
+  int64_t nC = (int64_t)chi * chi, nT = (int64_t)chi * d * chi;
+  int m = d < chi ? d : chi;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nC + nT; e += (int64_t)gridDim.x * blockDim.x) {
+    if (e < nC) {
+      int i = (int)(e % chi), j = (int)(e / chi);
+      double s = 0.0;
+      if (i < m && j < m)
+        for (int l = 0; l < d; ++l)
+          for (int k = 0; k < d; ++k) s += a[i + (int64_t)d * (j + (int64_t)d * (k + (int64_t)d * l))];
+      C[e] = s;
+    } else {
+      int64_t f = e - nC;
+      int i = (int)(f % chi), j = (int)((f / chi) % d), k = (int)(f / ((int64_t)chi * d));
+      double s = 0.0;
+      if (i < m && k < m)
+        for (int l = 0; l < d; ++l) s += a[i + (int64_t)d * (j + (int64_t)d * (k + (int64_t)d * l))];
+      T[f] = s;
+    }
+  }
+}
+
+void init_raw_dev(tnad_ctx* c, const double* a, int d, int chi, double* C, double* T) {
+  int64_t n = (int64_t)chi * chi + (int64_t)chi * d * chi;
+  k_init_raw<<<(int)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, c->stream>>>(a, d, chi, C, T);
+  count_launch(c);
+  check_launch(c, "init_raw");
+}
+
+__global__ void k_vals(const double* __restrict__ S, int64_t n, double* __restrict__ vals) {
+  double s0 = S[0];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    vals[i] = S[i] / s0;
+}
+
+// out = T + permute(T,(3,2,1)) for T χ×d×χ
+__global__ void k_sym_edge(const double* __restrict__ T, int chi, int d, double* __restrict__ out, double alpha,
+                           double beta) {
+  int64_t n = (int64_t)chi * d * chi;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t i = e % chi, j = (e / chi) % d, k = e / ((int64_t)chi * d);
+    double v = alpha * (T[e] + T[k + chi * (j + (int64_t)d * i)]);
+    out[e] = beta == 0.0 ? v : v + beta * out[e];
+  }
+}
+
+// Norm pullback of y = x/‖x‖ (src/autodiff.jl:23-29 + division rule):
+// dx = (dy − ⟨dy,y⟩·y)/‖x‖ with ‖x‖ and ⟨dy,y⟩ read from device scalars.
+__global__ void k_norm_bwd(int64_t n, const double* __restrict__ dy, const double* __restrict__ y,
+                           const double* __restrict__ nrm, const double* __restrict__ dot, double* __restrict__ dx) {
+  double inv = 1.0 / nrm[0], g = dot[0];
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+    dx[e] = (dy[e] - g * y[e]) * inv;
+}
+
+static int nb(int64_t n) { return (int)std::min<int64_t>((n + 255) / 256, 4096); }
+
+// ---------------------------------------------------------------------------
+// forward step
+// ---------------------------------------------------------------------------
+struct StepFwd {
+  Ten X1, X2, cp, w, y1, y2, Cn, Tn;
+  double *M = nullptr, *Cs = nullptr, *Ts = nullptr;
+  double *nC = nullptr, *nT = nullptr;  // device scalars
+};
+
+// cp = ein"ad,iba,dcl,jkcb -> ijlk"(corner, edge, edge, bulk)  (src/ctmrg.jl:130)
+static void grow(tnad_ctx* c, int prec, const Ten& a, const Ten& C, const Ten& T, StepFwd& f) {
+  int64_t chi = C.dim[0], d = a.dim[0];
+  f.X1.p = ws_d(c, chi * d * chi);
+  contract(c, prec, T, "iba", C, "ad", f.X1, "ibd");
+  f.X2.p = ws_d(c, chi * d * d * chi);
+  contract(c, prec, f.X1, "ibd", T, "dcl", f.X2, "ibcl");
+  f.cp.p = ws_d(c, chi * d * chi * d);
+  contract(c, prec, f.X2, "ibcl", a, "jkcb", f.cp, "ijlk");
+}
+
+// corner = ein"abcd,abi,cdj -> ij"(cp, z, z); edge = ein"abjcd,abi,dck -> ijk"(tp, z, z)
+// with tp = ein"iam,jkla -> ijklm"(edge, bulk) never materialised (src/ctmrg.jl:131,139-140).
+static void project(tnad_ctx* c, int prec, const Ten& a, const Ten& T, const Ten& z, StepFwd& f) {
+  int64_t chi = T.dim[0], d = a.dim[0];
+  f.w.p = ws_d(c, chi * chi * d);
+  contract(c, prec, f.cp, "abcd", z, "abi", f.w, "icd");
+  f.Cn.p = ws_d(c, chi * chi);
+  contract(c, prec, f.w, "icd", z, "cdj", f.Cn, "ij");
+  f.y1.p = ws_d(c, d * chi * d * chi);
+  contract(c, prec, T, "aed", z, "abi", f.y1, "edbi");
+  f.y2.p = ws_d(c, d * chi * d * chi);
+  contract(c, prec, f.y1, "edbi", a, "bjce", f.y2, "dijc");
+  f.Tn.p = ws_d(c, chi * d * chi);
+  contract(c, prec, f.y2, "dijc", z, "dck", f.Tn, "ijk");
+}
+
+// symmetrise + normalise (src/ctmrg.jl:145-150) into Cout/Tout
+static void finish(tnad_ctx* c, int64_t chi, int64_t d, StepFwd& f, double* Cout, double* Tout) {
+  f.Cs = ws_d(c, chi * chi);
+  f.Ts = ws_d(c, chi * d * chi);
+  add_transpose(c, chi, f.Cn.p, f.Cs);
+  k_sym_edge<<<nb(chi * d * chi), 256, 0, c->stream>>>(f.Tn.p, (int)chi, (int)d, f.Ts, 1.0, 0.0);
+  count_launch(c);
+  f.nC = ws_d(c, 2);
+  f.nT = ws_d(c, 2);
+  copy_d2d(c, Cout, f.Cs, chi * chi);
+  copy_d2d(c, Tout, f.Ts, chi * d * chi);
+  normalize_inplace(c, Cout, chi * chi, f.nC);
+  normalize_inplace(c, Tout, chi * d * chi, f.nT);
+}
+
+void ctmrg_step_fwd(tnad_ctx* c, int prec, const double* a_, int d, int chi, const double* C_, const double* T_,
+                    double* Cn, double* Tn, double* vals, double* U, double* S, double* V) {
+  WsScope scope(c);
+  const int64_t n = (int64_t)chi * d;
+  Ten a = make_ten(const_cast<double*>(a_), {d, d, d, d});
+  Ten C = make_ten(const_cast<double*>(C_), {chi, chi});
+  Ten T = make_ten(const_cast<double*>(T_), {chi, d, chi});
+  StepFwd f;
+  grow(c, prec, a, C, T, f);
+  // cpmat = reshape(cp, χD, χD); cpmat += cpmat'; u,s,v = svd(cpmat)   (:134-136)
+  f.M = ws_d(c, n * n);
+  add_transpose(c, n, f.cp.p, f.M);
+  svd_jacobi(c, f.M, n, n, U, S, V, true);
+  Ten z = make_ten(U, {chi, d, chi});  // z = reshape(u[:, 1:χ], χ, D, χ)  (:137)
+  project(c, prec, a, T, z, f);
+  if (vals) {
+    k_vals<<<nb(n), 256, 0, c->stream>>>(S, n, vals);  // vals = s ./ s[1]  (:142)
+    count_launch(c);
+  }
+  finish(c, chi, d, f, Cn, Tn);
+}
+
+// ---------------------------------------------------------------------------
+// pullback of one step
+// ---------------------------------------------------------------------------
+void ctmrg_step_bwd(tnad_ctx* c, int prec, const double* a_, int d, int chi, const double* C_, const double* T_,
+                    const double* U, const double* S, const double* V, const double* dCn_, const double* dTn_,
+                    double* dbulk, double* dC, double* dT, bool accumulate_bulk) {
+  WsScope scope(c);
+  const int64_t n = (int64_t)chi * d;
+  const int64_t nCh = (int64_t)chi * chi, nTe = (int64_t)chi * d * chi;
+  Ten a = make_ten(const_cast<double*>(a_), {d, d, d, d});
+  Ten C = make_ten(const_cast<double*>(C_), {chi, chi});
+  Ten T = make_ten(const_cast<double*>(T_), {chi, d, chi});
+  Ten z = make_ten(const_cast<double*>(U), {chi, d, chi});
+  // recompute the forward intermediates (the decomposition comes from the tape)
+  StepFwd f;
+  grow(c, prec, a, C, T, f);
+  project(c, prec, a, T, z, f);
+  double* Cout = ws_d(c, nCh);
+  double* Tout = ws_d(c, nTe);
+  finish(c, chi, d, f, Cout, Tout);
+  // normalise pullback: dCs = (dC' − ⟨dC',C'⟩C')/‖Cs‖
+  double* dots = ws_d(c, 2);
+  dot_dev(c, dCn_, Cout, nCh, dots);
+  dot_dev(c, dTn_, Tout, nTe, dots + 1);
+  double* dCs = ws_d(c, nCh);
+  double* dTs = ws_d(c, nTe);
+  k_norm_bwd<<<nb(nCh), 256, 0, c->stream>>>(nCh, dCn_, Cout, f.nC, dots, dCs);
+  k_norm_bwd<<<nb(nTe), 256, 0, c->stream>>>(nTe, dTn_, Tout, f.nT, dots + 1, dTs);
+  count_launch(c, 2);
+  // symmetrisation pullback: dCn = dCs + dCsᵀ ; dTn = dTs + permute(dTs,(3,2,1))
+  Ten dCn = make_ten(ws_d(c, nCh), {chi, chi});
+  Ten dTn = make_ten(ws_d(c, nTe), {chi, d, chi});
+  add_transpose(c, chi, dCs, dCn.p);
+  k_sym_edge<<<nb(nTe), 256, 0, c->stream>>>(dTs, chi, d, dTn.p, 1.0, 0.0);
+  count_launch(c);
+
+  Ten dz = make_ten(ws_d(c, n * chi), {chi, d, chi});
+  Ten dT_ = make_ten(dT, {chi, d, chi});
+  Ten dC_ = make_ten(dC, {chi, chi});
+  Ten da = make_ten(dbulk, {d, d, d, d});
+  const double bb = accumulate_bulk ? 1.0 : 0.0;
+  // edge = ein"dijc,dck->ijk"(y2, z)
+  Ten dy2 = make_ten(ws_d(c, f.y2.numel()), {d, chi, d, chi});
+  contract(c, prec, dTn, "ijk", z, "dck", dy2, "dijc");
+  contract(c, prec, f.y2, "dijc", dTn, "ijk", dz, "dck");
+  // y2 = ein"edbi,bjce->dijc"(y1, a)
+  Ten dy1 = make_ten(ws_d(c, f.y1.numel()), {d, chi, d, chi});
+  contract(c, prec, dy2, "dijc", a, "bjce", dy1, "edbi");
+  contract(c, prec, f.y1, "edbi", dy2, "dijc", da, "bjce", 1.0, bb);
+  // y1 = ein"aed,abi->edbi"(T, z)
+  contract(c, prec, dy1, "edbi", z, "abi", dT_, "aed");
+  contract(c, prec, T, "aed", dy1, "edbi", dz, "abi", 1.0, 1.0);
+  // corner = ein"icd,cdj->ij"(w, z)
+  Ten dw = make_ten(ws_d(c, f.w.numel()), {chi, chi, d});
+  contract(c, prec, dCn, "ij", z, "cdj", dw, "icd");
+  contract(c, prec, f.w, "icd", dCn, "ij", dz, "cdj", 1.0, 1.0);
+  // w = ein"abcd,abi->icd"(cp, z)
+  Ten dcp = make_ten(ws_d(c, n * n), {chi, d, chi, d});
+  contract(c, prec, dw, "icd", z, "abi", dcp, "abcd");
+  contract(c, prec, f.cp, "abcd", dw, "icd", dz, "abi", 1.0, 1.0);
+  // svd pullback with dU = [dz, 0]  (only u is used downstream: src/ctmrg.jl:137)
+  double* dUfull = ws_d(c, n * n);
+  fill(c, dUfull, n * n, 0.0);
+  copy_d2d(c, dUfull, dz.p, n * chi);
+  double* dM = ws_d(c, n * n);
+  svd_back(c, prec, U, S, V, n, n, dUfull, nullptr, nullptr, 1e-40, dM);
+  // cpmat += cpmat'  →  dcp += dM + dMᵀ
+  double* dMs = ws_d(c, n * n);
+  add_transpose(c, n, dM, dMs);
+  axpby(c, n * n, 1.0, dMs, 1.0, dcp.p);
+  // cp = ein"ibcl,jkcb->ijlk"(X2, a)
+  Ten dX2 = make_ten(ws_d(c, f.X2.numel()), {chi, d, d, chi});
+  contract(c, prec, dcp, "ijlk", a, "jkcb", dX2, "ibcl");
+  contract(c, prec, f.X2, "ibcl", dcp, "ijlk", da, "jkcb", 1.0, 1.0);
+  // X2 = ein"ibd,dcl->ibcl"(X1, T)
+  Ten dX1 = make_ten(ws_d(c, f.X1.numel()), {chi, d, chi});
+  contract(c, prec, dX2, "ibcl", T, "dcl", dX1, "ibd");
+  contract(c, prec, f.X1, "ibd", dX2, "ibcl", dT_, "dcl", 1.0, 1.0);
+  // X1 = ein"iba,ad->ibd"(T, C)
+  contract(c, prec, dX1, "ibd", C, "ad", dT_, "iba", 1.0, 1.0);
+  contract(c, prec, T, "iba", dX1, "ibd", dC_, "ad");
+}
+
+// ---------------------------------------------------------------------------
+// loop
+// ---------------------------------------------------------------------------
+__global__ void k_diffsq_partial(const double* __restrict__ v, const double* __restrict__ o, int64_t n,
+                                 double* __restrict__ out) {
+  // single block: Σ (v−o)²
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    double t = v[i] - o[i];
+    s += t * t;
+  }
+  __shared__ double sh[256];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+    if ((int)threadIdx.x < k) sh[threadIdx.x] += sh[threadIdx.x + k];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = sqrt(sh[0]);
+}
+
+CtmrgRun ctmrg_run(tnad_ctx* c, int prec, const double* a, int d, int chi, double* C, double* T, double tol,
+                   int maxit, CtmrgTape* tape, DevPool* pool, int64_t tape_budget) {
+  const int64_t n = (int64_t)chi * d;
+  const int64_t nCh = (int64_t)chi * chi, nTe = (int64_t)chi * d * chi;
+  WsScope scope(c);
+  double* U = ws_d(c, n * n);
+  double* S = ws_d(c, n);
+  double* V = ws_d(c, n * n);
+  double* vals = ws_d(c, n);
+  double* oldvals = ws_d(c, n);
+  double* Cn = ws_d(c, nCh);
+  double* Tn = ws_d(c, nTe);
+  double* diff = ws_d(c, 1);
+  if (tape) {
+    tape->d = d;
+    tape->chi = chi;
+    tape->prec = prec;
+    tape->a = a;
+  }
+  int64_t used = 0;
+  CtmrgRun run;
+  int counter = 0;  // StopFunction(oldvals, -1, ...) has seen state 0
+  bool have_old = false;
+  while (true) {
+    if (tape) {
+      double* Ck = pool->d(nCh);
+      double* Tk = pool->d(nTe);
+      copy_d2d(c, Ck, C, nCh);
+      copy_d2d(c, Tk, T, nTe);
+      tape->C.push_back(Ck);
+      tape->T.push_back(Tk);
+    }
+    ctmrg_step_fwd(c, prec, a, d, chi, C, T, Cn, Tn, vals, U, S, V);
+    if (tape) {
+      int64_t need = (2 * n * n + n) * 8;
+      if (used + need <= tape_budget) {
+        double* Uk = pool->d(n * n);
+        double* Sk = pool->d(n);
+        double* Vk = pool->d(n * n);
+        copy_d2d(c, Uk, U, n * n);
+        copy_d2d(c, Sk, S, n);
+        copy_d2d(c, Vk, V, n * n);
+        tape->U.push_back(Uk);
+        tape->S.push_back(Sk);
+        tape->V.push_back(Vk);
+        used += need;
+      } else {
+        tape->U.push_back(nullptr);
+        tape->S.push_back(nullptr);
+        tape->V.push_back(nullptr);
+      }
+    }
+    copy_d2d(c, C, Cn, nCh);
+    copy_d2d(c, T, Tn, nTe);
+    run.steps++;
+    counter++;
+    if (counter > maxit) break;
+    double dv = std::numeric_limits<double>::infinity();
+    if (have_old) {
+      k_diffsq_partial<<<1, 256, 0, c->stream>>>(vals, oldvals, n, diff);
+      count_launch(c);
+      TNAD_CK(cudaMemcpyAsync(c->h_pin, diff, 8, cudaMemcpyDeviceToHost, c->stream));
+      TNAD_CK(cudaStreamSynchronize(c->stream));
+      dv = c->h_pin[0];
+    }
+    run.last_diff = dv;
+    if (dv <= tol) break;
+    copy_d2d(c, oldvals, vals, n);
+    have_old = true;
+  }
+  if (tape) tape->steps = run.steps;
+  return run;
+}
+
+void ctmrg_reverse(tnad_ctx* c, const CtmrgTape& tape, double* dC, double* dT, double* dbulk) {
+  const int d = tape.d, chi = tape.chi;
+  const int64_t n = (int64_t)chi * d;
+  const int64_t nCh = (int64_t)chi * chi, nTe = (int64_t)chi * d * chi;
+  WsScope scope(c);
+  double* dCp = ws_d(c, nCh);
+  double* dTp = ws_d(c, nTe);
+  double* Ut = nullptr;
+  double* St = nullptr;
+  double* Vt = nullptr;
+  for (int k = tape.steps - 1; k >= 0; --k) {
+    const double* U = tape.U[k];
+    const double* S = tape.S[k];
+    const double* V = tape.V[k];
+    WsScope inner(c);
+    if (!U) {
+      // checkpoint recompute: rebuild the decomposition from (C_k, T_k)
+      Ut = ws_d(c, n * n);
+      St = ws_d(c, n);
+      Vt = ws_d(c, n * n);
+      double* Cn = ws_d(c, nCh);
+      double* Tn = ws_d(c, nTe);
+      ctmrg_step_fwd(c, tape.prec, tape.a, d, chi, tape.C[k], tape.T[k], Cn, Tn, nullptr, Ut, St, Vt);
+      U = Ut;
+      S = St;
+      V = Vt;
+    }
+    ctmrg_step_bwd(c, tape.prec, tape.a, d, chi, tape.C[k], tape.T[k], U, S, V, dC, dT, dbulk, dCp, dTp, true);
+    copy_d2d(c, dC, dCp, nCh);
+    copy_d2d(c, dT, dTp, nTe);
+  }
+}
+
+}  // namespace tnad

@@ -1,0 +1,154 @@
+// FP64 (DFMA) GEMM of the plain path.  Column-major, op(A)/op(B) ∈ {N,T}.
+// GB300 issues FP64 at a small fraction of its FP32/tensor rate, so this kernel
+// is bound by the DFMA pipe: register-tiled TM×TN micro-tiles over a BM×BN×16
+// shared-memory tile, deterministic split-K (fixed-order partial sums) when the
+// output has too few tiles to fill the 152 SMs.
+#include <algorithm>
+
+#include "tnad_internal.h"
+
+namespace tnad {
+
+template <int BM, int BN, int TM, int TN>
+__global__ void __launch_bounds__((BM / TM) * (BN / TN))
+    k_gemm_f64(int ta, int tb, int64_t M, int64_t N, int64_t K, int64_t kchunk, double alpha,
+               const double* __restrict__ A, int64_t lda, const double* __restrict__ B, int64_t ldb,
+               double beta, double* __restrict__ C, int64_t ldc, double* __restrict__ Cpart) {
+  constexpr int BK = 16;
+  constexpr int NT = (BM / TM) * (BN / TN);
+  __shared__ double As[BK][BM + 1];
+  __shared__ double Bs[BK][BN + 1];
+  const int tid = threadIdx.x;
+  const int64_t m0 = (int64_t)blockIdx.x * BM, n0 = (int64_t)blockIdx.y * BN;
+  const int64_t kbeg = (int64_t)blockIdx.z * kchunk;
+  const int64_t kend = min(K, kbeg + kchunk);
+  const int tr = (tid % (BM / TM)) * TM;
+  const int tc = (tid / (BM / TM)) * TN;
+  double acc[TM][TN];
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) acc[i][j] = 0.0;
+
+  for (int64_t k0 = kbeg; k0 < kend; k0 += BK) {
+    // A tile: op(A)(i,k), i in [m0,m0+BM), k in [k0,k0+BK)
+    for (int e = tid; e < BM * BK; e += NT) {
+      int i, k;
+      if (!ta) { i = e % BM; k = e / BM; } else { k = e % BK; i = e / BK; }
+      int64_t gi = m0 + i, gk = k0 + k;
+      double v = 0.0;
+      if (gi < M && gk < kend) v = !ta ? A[gi + gk * lda] : A[gk + gi * lda];
+      As[k][i] = v;
+    }
+    for (int e = tid; e < BN * BK; e += NT) {
+      int j, k;
+      if (!tb) { k = e % BK; j = e / BK; } else { j = e % BN; k = e / BN; }
+      int64_t gj = n0 + j, gk = k0 + k;
+      double v = 0.0;
+      if (gj < N && gk < kend) v = !tb ? B[gk + gj * ldb] : B[gj + gk * ldb];
+      Bs[k][j] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < BK; ++k) {
+      double a[TM], b[TN];
+#pragma unroll
+      for (int i = 0; i < TM; ++i) a[i] = As[k][tr + i];
+#pragma unroll
+      for (int j = 0; j < TN; ++j) b[j] = Bs[k][tc + j];
+#pragma unroll
+      for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+  if (Cpart) {
+    double* P = Cpart + (int64_t)blockIdx.z * M * N;
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+#pragma unroll
+      for (int j = 0; j < TN; ++j) {
+        int64_t gi = m0 + tr + i, gj = n0 + tc + j;
+        if (gi < M && gj < N) P[gi + gj * M] = acc[i][j];
+      }
+  } else {
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+#pragma unroll
+      for (int j = 0; j < TN; ++j) {
+        int64_t gi = m0 + tr + i, gj = n0 + tc + j;
+        if (gi < M && gj < N) {
+          double v = alpha * acc[i][j];
+          C[gi + gj * ldc] = beta == 0.0 ? v : v + beta * C[gi + gj * ldc];
+        }
+      }
+  }
+}
+
+__global__ void k_splitk_reduce(int64_t M, int64_t N, int ks, const double* __restrict__ P, double alpha,
+                                double beta, double* __restrict__ C, int64_t ldc) {
+  int64_t MN = M * N;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < MN; e += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int z = 0; z < ks; ++z) s += P[e + z * MN];
+    int64_t i = e % M, j = e / M;
+    double v = alpha * s;
+    C[i + j * ldc] = beta == 0.0 ? v : v + beta * C[i + j * ldc];
+  }
+}
+
+void gemm_f64(tnad_ctx* c, char ta, char tb, int64_t M, int64_t N, int64_t K, double alpha, const double* A,
+              int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc) {
+  if (M <= 0 || N <= 0) return;
+  if (K <= 0) {
+    if (beta == 0.0) {
+      for (int64_t j = 0; j < N; ++j) fill(c, C + j * ldc, M, 0.0);
+    } else if (beta != 1.0) {
+      for (int64_t j = 0; j < N; ++j) scale(c, M, beta, C + j * ldc);
+    }
+    return;
+  }
+  int ita = (ta == 'T' || ta == 't'), itb = (tb == 'T' || tb == 't');
+  const bool big = (M >= 64 && N >= 64);
+  const int BM = big ? 64 : 32, BN = big ? 64 : 32;
+  int64_t tiles = ((M + BM - 1) / BM) * ((N + BN - 1) / BN);
+  int ks = 1;
+  if (tiles < c->sm_count && K >= 512) {
+    int64_t want = (2 * c->sm_count + tiles - 1) / tiles;
+    int64_t cap = K / 256;
+    ks = (int)std::max<int64_t>(1, std::min<int64_t>({want, cap, 64}));
+  }
+  int64_t kchunk = (K + ks - 1) / ks;
+  kchunk = (kchunk + 15) / 16 * 16;
+  ks = (int)((K + kchunk - 1) / kchunk);
+  WsScope scope(c);
+  double* part = nullptr;
+  if (ks > 1) part = ws_d(c, (int64_t)ks * M * N);
+  dim3 grid((unsigned)((M + BM - 1) / BM), (unsigned)((N + BN - 1) / BN), (unsigned)ks);
+  if (big)
+    k_gemm_f64<64, 64, 4, 4><<<grid, 256, 0, c->stream>>>(ita, itb, M, N, K, kchunk, alpha, A, lda, B, ldb, beta, C,
+                                                          ldc, part);
+  else
+    k_gemm_f64<32, 32, 2, 2><<<grid, 256, 0, c->stream>>>(ita, itb, M, N, K, kchunk, alpha, A, lda, B, ldb, beta, C,
+                                                          ldc, part);
+  count_launch(c);
+  check_launch(c, "gemm_f64");
+  if (ks > 1) {
+    int64_t MN = M * N;
+    int nb = (int)std::min<int64_t>((MN + 255) / 256, 4096);
+    k_splitk_reduce<<<nb, 256, 0, c->stream>>>(M, N, ks, part, alpha, beta, C, ldc);
+    count_launch(c);
+    check_launch(c, "splitk_reduce");
+  }
+}
+
+void gemm(tnad_ctx* c, int prec, char ta, char tb, int64_t M, int64_t N, int64_t K, double alpha, const double* A,
+          int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc) {
+  if (prec == TNAD_PREC_TF32X3 && c->tc_ok)
+    gemm_tf32x3(c, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+  else
+    gemm_f64(c, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+
+}  // namespace tnad

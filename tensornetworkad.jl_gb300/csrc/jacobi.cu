@@ -1,0 +1,311 @@
+// FP64 one-sided (Hestenes) Jacobi SVD: the decomposition of src/ctmrg.jl:136
+// and src/trg.jl:36 (LinearAlgebra.svd).  GB300 has a narrow FP64 pipe, so the
+// schedule spreads every round over all SMs: a round of the circle-method
+// tournament pairs all columns at once, one warp per column pair (three dot
+// products by warp shuffle, one plane rotation of W and V).  A sweep is n−1
+// rounds; sweeps repeat until no pair needed a rotation (relative
+// orthogonality ≤ m·ε), capped at kMaxSweeps (→ TNAD_ERR_NOT_CONVERGED).
+// Singular values are the column norms, sorted descending by a rank kernel
+// (ties by index, so the result is deterministic).
+#include <cfloat>
+#include <cmath>
+
+#include "tnad_internal.h"
+
+namespace tnad {
+
+static const int kMaxSweeps = 100;
+static const int kRelSweeps = 20;
+
+__device__ __forceinline__ double wsum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ void pair_of(int r, int k, int NP, int* p, int* q) {
+  // circle method over NP (even) players; round r in [0, NP-1), pair k in [0, NP/2)
+  if (k == 0) {
+    *p = NP - 1;
+    *q = r;
+  } else {
+    *p = (r + k) % (NP - 1);
+    *q = (r - k + (NP - 1)) % (NP - 1);
+  }
+}
+
+__global__ void k_jacobi_round(double* __restrict__ W, double* __restrict__ V, int64_t m, int64_t n, int r, int NP,
+                               double tol, double abs_eps, const double* __restrict__ fro2, int* __restrict__ rotated) {
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (warp >= NP / 2) return;
+  int p, q;
+  pair_of(r, warp, NP, &p, &q);
+  if (p >= n || q >= n) return;  // bye
+  if (p > q) {
+    int t = p;
+    p = q;
+    q = t;
+  }
+  double* wp = W + (int64_t)p * m;
+  double* wq = W + (int64_t)q * m;
+  double a = 0.0, b = 0.0, g = 0.0;
+  for (int64_t i = lane; i < m; i += 32) {
+    double x = wp[i], y = wq[i];
+    a = fma(x, x, a);
+    b = fma(y, y, b);
+    g = fma(x, y, g);
+  }
+  a = wsum(a);
+  b = wsum(b);
+  g = wsum(g);
+  if (g == 0.0 || a == 0.0 || b == 0.0) return;
+  // Stop rule: relative orthogonality m·ε, plus the rounding floor.  Every
+  // rotation against a large column leaves noise of size ~ε·‖A‖ in a small one,
+  // so |γ| cannot drop below ~ε·‖A‖_F·(‖w_p‖+‖w_q‖); rotating below that only
+  // reshuffles noise (and never terminates on graded spectra such as TRG's).
+  if (fabs(g) <= tol * sqrt(a) * sqrt(b) + abs_eps * sqrt(fro2[0]) * (sqrt(a) + sqrt(b))) return;
+  double zeta = (b - a) / (2.0 * g);
+  double t;
+  if (fabs(zeta) > 1e150)
+    t = 0.5 / zeta;
+  else
+    t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+  double cs = 1.0 / sqrt(1.0 + t * t);
+  double sn = cs * t;
+  for (int64_t i = lane; i < m; i += 32) {
+    double x = wp[i], y = wq[i];
+    wp[i] = cs * x - sn * y;
+    wq[i] = sn * x + cs * y;
+  }
+  double* vp = V + (int64_t)p * n;
+  double* vq = V + (int64_t)q * n;
+  for (int64_t i = lane; i < n; i += 32) {
+    double x = vp[i], y = vq[i];
+    vp[i] = cs * x - sn * y;
+    vq[i] = sn * x + cs * y;
+  }
+  if (lane == 0) atomicAdd(rotated, 1);
+}
+
+__global__ void k_eye(double* V, int64_t n) {
+  int64_t nn = n * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nn; e += (int64_t)gridDim.x * blockDim.x)
+    V[e] = (e % n == e / n) ? 1.0 : 0.0;
+}
+
+// s_j = ‖W_j‖ ; sg_j = sign(V_j·W_j) (used for the null/weak columns of a symmetric A)
+__global__ void k_colnorms(const double* __restrict__ W, const double* __restrict__ Vw, int64_t m, int64_t n,
+                           double* __restrict__ s, double* __restrict__ sg) {
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  const double* w = W + (int64_t)warp * m;
+  const double* v = Vw + (int64_t)warp * n;
+  double a = 0.0, g = 0.0;
+  for (int64_t i = lane; i < m; i += 32) {
+    a = fma(w[i], w[i], a);
+    if (i < n) g = fma(v[i], w[i], g);
+  }
+  a = wsum(a);
+  g = wsum(g);
+  if (lane == 0) {
+    s[warp] = sqrt(a);
+    sg[warp] = g < 0.0 ? -1.0 : 1.0;
+  }
+}
+
+// rank[j] = #{i : s_i > s_j or (s_i == s_j and i < j)}  → descending order
+__global__ void k_rank(const double* __restrict__ s, int64_t n, int* __restrict__ rank) {
+  int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  double sj = s[j];
+  int r = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    double si = s[i];
+    r += (si > sj || (si == sj && i < j)) ? 1 : 0;
+  }
+  rank[j] = r;
+}
+
+// Scatter sorted: S[rank j] = ‖W_j‖, V_out[:, rank j] = V_j and
+//  - symmetric A: U[:, rank j] = sign(V_j·W_j)·V_j — the left vectors of a
+//    symmetric matrix are its signed right vectors, and V (a product of plane
+//    rotations) is orthogonal to working precision, including null columns;
+//  - general A: U[:, rank j] = W_j/‖W_j‖; columns below weak_rel·‖A‖_F (whose
+//    direction carries the ε·‖A‖ rounding noise) are counted and afterwards
+//    re-orthonormalised against all larger ones by k_complete_col.
+__global__ void k_scatter(const double* __restrict__ W, const double* __restrict__ Vw, const double* __restrict__ s,
+                          const double* __restrict__ sg, const int* __restrict__ rank, int64_t m, int64_t n,
+                          int symmetric, double weak_rel, const double* __restrict__ fro2, double* __restrict__ U,
+                          double* __restrict__ S, double* __restrict__ Vout, int* __restrict__ nweak) {
+  int64_t j = blockIdx.y;
+  int r = rank[j];
+  double sj = s[j];
+  bool weak = !(sj > weak_rel * sqrt(fro2[0])) || !(sj > 1e-300);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+    double u;
+    if (symmetric)
+      u = i < n ? sg[j] * Vw[i + j * n] : 0.0;
+    else
+      u = sj > 1e-300 ? W[i + j * m] / sj : 0.0;
+    U[i + (int64_t)r * m] = u;
+  }
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    Vout[i + (int64_t)r * n] = Vw[i + j * n];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    S[r] = sj > 1e-300 ? sj : 0.0;
+    if (weak && !symmetric) atomicAdd(nweak, 1);
+  }
+}
+
+// Re-orthonormalisation of a weak column k of U (general matrices): start from
+// the column itself (or e_pick, the unit vector least covered by columns
+// 0..k-1, when it is zero); two rounds of classical Gram-Schmidt against
+// columns 0..k-1; normalise.  One CTA per column, columns in order.
+__global__ void k_complete_col(double* __restrict__ U, int64_t m, int64_t k, double* __restrict__ coef) {
+  extern __shared__ double sh[];
+  double* x = sh;  // m
+  __shared__ double red[32];
+  __shared__ int pick;
+  // choose the unit vector e_i with the smallest projection onto span(U[:,0:k])
+  if (threadIdx.x == 0) pick = -1;
+  __syncthreads();
+  double best = 2.0;
+  int bi = 0;
+  for (int64_t i = threadIdx.x; i < m; i += blockDim.x) {
+    double p = 0.0;
+    for (int64_t c = 0; c < k; ++c) p += U[i + c * m] * U[i + c * m];
+    if (p < best) { best = p; bi = (int)i; }
+  }
+  // block argmin (first index on ties)
+  __shared__ double bv[1024];
+  __shared__ int bix[1024];
+  bv[threadIdx.x] = best;
+  bix[threadIdx.x] = bi;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      if (bv[threadIdx.x + s] < bv[threadIdx.x] ||
+          (bv[threadIdx.x + s] == bv[threadIdx.x] && bix[threadIdx.x + s] < bix[threadIdx.x])) {
+        bv[threadIdx.x] = bv[threadIdx.x + s];
+        bix[threadIdx.x] = bix[threadIdx.x + s];
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) pick = bix[0];
+  __syncthreads();
+  // start from the current (noisy) column when it is non-zero, else from e_pick
+  __shared__ double nz;
+  if (threadIdx.x == 0) nz = 0.0;
+  __syncthreads();
+  double part = 0.0;
+  for (int64_t i = threadIdx.x; i < m; i += blockDim.x) part += fabs(U[i + k * m]);
+  part = wsum(part);
+  if ((threadIdx.x & 31) == 0) atomicAdd(&nz, part);
+  __syncthreads();
+  for (int64_t i = threadIdx.x; i < m; i += blockDim.x) x[i] = nz > 0.0 ? U[i + k * m] : ((i == pick) ? 1.0 : 0.0);
+  __syncthreads();
+  for (int pass = 0; pass < 2; ++pass) {
+    // coef[c] = U[:,c]·x
+    for (int64_t c = threadIdx.x >> 5; c < k; c += blockDim.x >> 5) {
+      double a = 0.0;
+      for (int64_t i = threadIdx.x & 31; i < m; i += 32) a += U[i + c * m] * x[i];
+      a = wsum(a);
+      if ((threadIdx.x & 31) == 0) coef[c] = a;
+    }
+    __syncthreads();
+    for (int64_t i = threadIdx.x; i < m; i += blockDim.x) {
+      double a = x[i];
+      for (int64_t c = 0; c < k; ++c) a -= U[i + c * m] * coef[c];
+      x[i] = a;
+    }
+    __syncthreads();
+  }
+  double a = 0.0;
+  for (int64_t i = threadIdx.x; i < m; i += blockDim.x) a += x[i] * x[i];
+  a = wsum(a);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = a;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    red[0] = sqrt(t);
+  }
+  __syncthreads();
+  double nrm = red[0];
+  for (int64_t i = threadIdx.x; i < m; i += blockDim.x) U[i + k * m] = x[i] / nrm;
+}
+
+void svd_jacobi(tnad_ctx* c, const double* A, int64_t m, int64_t n, double* U, double* S, double* V,
+                bool symmetric) {
+  TNAD_REQUIRE(m >= n && n >= 1, TNAD_ERR_SHAPE, "svd_jacobi: needs m >= n >= 1");
+  WsScope scope(c);
+  double* W = ws_d(c, m * n);
+  double* Vw = ws_d(c, n * n);
+  double* s = ws_d(c, n);
+  double* sg = ws_d(c, n);
+  double* fro2 = ws_d(c, 1);
+  int* rank = (int*)c->ws.alloc(n * sizeof(int));
+  copy_d2d(c, W, A, m * n);
+  sumsq_dev(c, A, m * n, fro2);
+  k_eye<<<(int)std::min<int64_t>((n * n + 255) / 256, 4096), 256, 0, c->stream>>>(Vw, n);
+  count_launch(c);
+  const int NP = (int)(n + (n & 1));
+  // Relative orthogonality target.  After a rotation the computed |γ|/√(αβ)
+  // is only as small as the rounding of an m-term dot product (~√m·ε on
+  // average, up to m·ε); a √m·ε target therefore keeps re-rotating noise-level
+  // columns forever.  m·ε still leaves U, V orthogonal far below 1e-10.
+  const double tol = (double)std::max<int64_t>(m, 16) * DBL_EPSILON;
+  const double abs_eps = 2.0 * DBL_EPSILON;
+  // General A: only exactly-null columns are rebuilt.  A tiny but non-zero
+  // column keeps U_j = W_j/s_j so that A·V_j = s_j·U_j holds exactly: trg_svd
+  // keeps one singular value at the rounding floor (its +1 quirk) and the
+  // √s pullback of that column needs a consistent triplet.
+  const double weak_rel = 0.0;
+  int* flag = c->d_flag;
+  bool converged = (n == 1);
+  const int threads = 256;
+  const int blocks = (NP / 2 * 32 + threads - 1) / threads;
+  for (int sweep = 0; sweep < kMaxSweeps && !converged; ++sweep) {
+    TNAD_CK(cudaMemsetAsync(flag, 0, sizeof(int), c->stream));
+    // Purely relative sweeps first: they drive null and noise-level columns to
+    // exact orthogonality (the triplets trg_svd's √s pullback relies on).  Only
+    // a spectrum that keeps re-rotating noise past kRelSweeps gets the floor.
+    const double ae = sweep < kRelSweeps ? 0.0 : abs_eps;
+    for (int r = 0; r < NP - 1; ++r) {
+      k_jacobi_round<<<blocks, threads, 0, c->stream>>>(W, Vw, m, n, r, NP, tol, ae, fro2, flag);
+    }
+    count_launch(c, NP - 1);
+    check_launch(c, "jacobi_round");
+    TNAD_CK(cudaMemcpyAsync(c->h_flag, flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    TNAD_CK(cudaStreamSynchronize(c->stream));
+    if (c->h_flag[0] == 0) converged = true;
+  }
+  TNAD_REQUIRE(converged, TNAD_ERR_NOT_CONVERGED, "svd_jacobi: no convergence within the sweep cap");
+  k_colnorms<<<(int)((n * 32 + 255) / 256), 256, 0, c->stream>>>(W, Vw, m, n, s, sg);
+  k_rank<<<(int)((n + 255) / 256), 256, 0, c->stream>>>(s, n, rank);
+  TNAD_CK(cudaMemsetAsync(flag + 1, 0, sizeof(int), c->stream));
+  dim3 g((unsigned)std::min<int64_t>((std::max(m, n) + 255) / 256, 16), (unsigned)n);
+  k_scatter<<<g, 256, 0, c->stream>>>(W, Vw, s, sg, rank, m, n, symmetric ? 1 : 0, weak_rel, fro2, U, S, V,
+                                      flag + 1);
+  count_launch(c, 3);
+  check_launch(c, "svd_scatter");
+  if (!symmetric) {
+    TNAD_CK(cudaMemcpyAsync(c->h_flag + 1, flag + 1, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    TNAD_CK(cudaStreamSynchronize(c->stream));
+    int nnull = c->h_flag[1];
+    if (nnull > 0) {
+      TNAD_REQUIRE(m <= 4096, TNAD_ERR_SHAPE, "svd_jacobi: weak-column completion limited to m <= 4096");
+      double* coef = ws_d(c, n);
+      for (int64_t k = n - nnull; k < n; ++k) {
+        k_complete_col<<<1, 1024, m * sizeof(double), c->stream>>>(U, m, k, coef);
+        count_launch(c);
+      }
+      check_launch(c, "svd_complete");
+    }
+  }
+}
+
+}  // namespace tnad

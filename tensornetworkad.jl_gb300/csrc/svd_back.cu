@@ -1,0 +1,74 @@
+// SVD adjoint of src/trg.jl:94-128 (real case).  The Lorentzian-broadened
+// F-matrix F_ij = (s_j²−s_i²)/((s_j²−s_i²)²+η) is formed in FP64 inside the
+// kernel that assembles res = (J+Jᵀ)S + S(K+Kᵀ) + diag(dS); the surrounding
+// products Uᵀ·dU, Vᵀ·dV, U·res·Vᵀ are GEMMs.
+#include "tnad_internal.h"
+
+namespace tnad {
+
+__global__ void k_svdback_res(int64_t n, const double* __restrict__ S, const double* __restrict__ X,
+                              const double* __restrict__ Y, const double* __restrict__ dS, double eta,
+                              double* __restrict__ res) {
+  int64_t nn = n * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nn; e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t i = e % n, j = e / n;
+    double si = S[i], sj = S[j];
+    // Explicitly rounded operations (no FMA contraction): the reference forms
+    // S2 = S.^2 first, so F_ii is exactly 0 and F_ji = −F_ij exactly; a fused
+    // sj*sj − si*si would leave a rounding residue whose 1/d blows up.
+    double d = __dsub_rn(__dmul_rn(sj, sj), __dmul_rn(si, si));  // S2' .- S2
+    double f = __ddiv_rn(d, __dadd_rn(__dmul_rn(d, d), eta));     // F_ij ; F_ji = −f
+    double r = 0.0;
+    if (X) r = __dadd_rn(r, __dmul_rn(__dadd_rn(__dmul_rn(f, X[i + j * n]), __dmul_rn(-f, X[j + i * n])), sj));
+    if (Y) r = __dadd_rn(r, __dmul_rn(si, __dadd_rn(__dmul_rn(f, Y[i + j * n]), __dmul_rn(-f, Y[j + i * n]))));
+    if (dS && i == j) r = __dadd_rn(r, dS[i]);
+    res[e] = r;
+  }
+}
+
+__global__ void k_scale_cols(int64_t m, int64_t n, double* __restrict__ P, const double* __restrict__ S, double eta) {
+  int64_t mn = m * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < mn; e += (int64_t)gridDim.x * blockDim.x) {
+    double s = S[e / m];
+    P[e] *= s / (s * s + eta);
+  }
+}
+
+void svd_back(tnad_ctx* c, int prec, const double* U, const double* S, const double* V, int64_t m, int64_t n,
+              const double* dU, const double* dS, const double* dV, double eta, double* dA) {
+  WsScope scope(c);
+  if (!dU && !dS && !dV) {
+    fill(c, dA, m * n, 0.0);
+    return;
+  }
+  double* X = nullptr;
+  double* Y = nullptr;
+  if (dU) {
+    X = ws_d(c, n * n);
+    gemm(c, prec, 'T', 'N', n, n, m, 1.0, U, m, dU, m, 0.0, X, n);
+  }
+  if (dV) {
+    Y = ws_d(c, n * n);
+    gemm(c, prec, 'T', 'N', n, n, n, 1.0, V, n, dV, n, 0.0, Y, n);
+  }
+  double* res = ws_d(c, n * n);
+  int nb = (int)std::min<int64_t>((n * n + 255) / 256, 4096);
+  k_svdback_res<<<nb, 256, 0, c->stream>>>(n, S, X, Y, dS, eta, res);
+  count_launch(c);
+  check_launch(c, "svdback_res");
+  double* T1 = ws_d(c, m * n);
+  gemm(c, prec, 'N', 'N', m, n, n, 1.0, U, m, res, n, 0.0, T1, m);
+  gemm(c, prec, 'N', 'T', m, n, n, 1.0, T1, m, V, n, 0.0, dA, m);
+  if (dU && m != n) {
+    // (dU − U·(Uᵀ·dU))·diag(Sinv)·Vᵀ   src/trg.jl:120-122
+    double* P = ws_d(c, m * n);
+    copy_d2d(c, P, dU, m * n);
+    gemm(c, prec, 'N', 'N', m, n, n, -1.0, U, m, X, n, 1.0, P, m);
+    int nb2 = (int)std::min<int64_t>((m * n + 255) / 256, 4096);
+    k_scale_cols<<<nb2, 256, 0, c->stream>>>(m, n, P, S, eta);
+    count_launch(c);
+    gemm(c, prec, 'N', 'T', m, n, n, 1.0, P, m, V, n, 1.0, dA, m);
+  }
+}
+
+}  // namespace tnad

@@ -1,0 +1,37 @@
+// Energy driver state shared by energy.cu and the C ABI.
+#pragma once
+
+#include "tnad_drivers.h"
+
+namespace tnad {
+
+// Intermediates of expectationvalue (src/variationalipeps.jl:49-56), workspace-backed.
+struct Expect {
+  double* apn = nullptr;  // ap/‖ap‖
+  double* nap = nullptr;  // ‖ap‖ (device scalar)
+  Ten w1, w2, r, v, l, G;
+  double* sc = nullptr;  // {E, e, n}
+};
+
+struct EnergyTape {
+  int D = 0, s = 0, chi = 0, d = 0, steps = 0, prec = TNAD_PREC_FP64;
+  double E = 0.0;
+  DevPool pool;
+  double *h = nullptr, *As = nullptr, *nA = nullptr, *ap = nullptr, *a = nullptr;
+  double *C = nullptr, *T = nullptr;  // converged environment
+  CtmrgTape ct;
+};
+
+void symmetrize_fwd(tnad_ctx* c, const double* A, int D, int s, double* As, double* nA_dev);
+void symmetrize_bwd(tnad_ctx* c, const double* As, const double* nA_dev, int D, int s, const double* dAs,
+                    double* dA);
+void double_layer(tnad_ctx* c, const double* As, int D, int s, double* ap, double* bulk);
+void expect_fwd(tnad_ctx* c, int prec, const double* h, const double* ap, int d, int s, int chi, const double* C,
+                const double* T, Expect& x);
+void expect_bwd(tnad_ctx* c, int prec, const double* h, int d, int s, int chi, const double* C, const double* T,
+                const Expect& x, double dE, double* dap, double* dC, double* dT);
+void energy_fwd(tnad_ctx* c, EnergyTape& tp, const double* h, const double* A, int D, int s, int chi, double tol,
+                int maxit, const tnad_opts& o, const double* Cinit, const double* Tinit, bool record);
+void energy_bwd(tnad_ctx* c, EnergyTape& tp, double dE, double* dA);
+
+}  // namespace tnad

@@ -1,0 +1,164 @@
+// Internal declarations of libtnad: context, device workspace, tensors and the
+// kernel entry points shared between translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "tnad.h"
+
+namespace tnad {
+
+struct Error {
+  int code;
+  std::string msg;
+};
+
+[[noreturn]] void fail(int code, const std::string& msg);
+
+#define TNAD_CK(x)                                                                  \
+  do {                                                                              \
+    cudaError_t e_ = (x);                                                           \
+    if (e_ != cudaSuccess)                                                          \
+      ::tnad::fail(TNAD_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+#define TNAD_REQUIRE(cond, code, msg) \
+  do {                                \
+    if (!(cond)) ::tnad::fail(code, msg); \
+  } while (0)
+
+// Stack-ordered device workspace over persistent chunks.  alloc() bumps, and
+// a Mark restores the stack (chunks are kept for reuse until ctx destruction).
+class Arena {
+ public:
+  struct Mark {
+    size_t chunk;
+    size_t used;
+  };
+  void* alloc(size_t bytes);
+  Mark mark() const;
+  void reset(const Mark& m);
+  void release_all();
+  int64_t bytes_held() const;
+
+ private:
+  struct Chunk {
+    char* base;
+    size_t cap;
+    size_t used;
+  };
+  std::vector<Chunk> chunks_;
+  size_t cur_ = 0;
+};
+
+// A column-major FP64 tensor view on the device.
+struct Ten {
+  double* p = nullptr;
+  int nd = 0;
+  int64_t dim[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  int64_t numel() const {
+    int64_t n = 1;
+    for (int i = 0; i < nd; ++i) n *= dim[i];
+    return n;
+  }
+};
+Ten make_ten(double* p, std::initializer_list<int64_t> dims);
+
+}  // namespace tnad
+
+struct tnad_ctx {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t stream = nullptr;
+  tnad::Arena ws;
+  std::string err;
+  int64_t launches = 0;
+  double* d_red = nullptr;  // small device scratch for reductions (4096 doubles)
+  double* h_pin = nullptr;  // pinned host mirror (64 doubles)
+  int* d_flag = nullptr;    // device flags / counters (64 ints)
+  int* h_flag = nullptr;    // pinned host mirror of the flags
+  bool tc_ok = false;       // tcgen05 GEMM path available (sm_100 family)
+};
+
+namespace tnad {
+
+// RAII scope over the context's workspace stack.
+struct WsScope {
+  tnad_ctx* c;
+  Arena::Mark m;
+  explicit WsScope(tnad_ctx* ctx) : c(ctx), m(ctx->ws.mark()) {}
+  ~WsScope() { c->ws.reset(m); }
+};
+inline double* ws_d(tnad_ctx* c, int64_t n) { return (double*)c->ws.alloc((size_t)n * 8); }
+inline float* ws_f(tnad_ctx* c, int64_t n) { return (float*)c->ws.alloc((size_t)n * 4); }
+
+inline void count_launch(tnad_ctx* c, int n = 1) { c->launches += n; }
+void check_launch(tnad_ctx* c, const char* what);
+
+// ---------------- elementwise / reductions (elementwise.cu) ----------------
+void fill(tnad_ctx* c, double* x, int64_t n, double v);
+void copy_d2d(tnad_ctx* c, double* dst, const double* src, int64_t n);
+// y = a*x + b*y
+void axpby(tnad_ctx* c, int64_t n, double a, const double* x, double b, double* y);
+void scale(tnad_ctx* c, int64_t n, double a, double* x);
+// out = x + xᵀ for an n×n matrix (out may alias nothing)
+void add_transpose(tnad_ctx* c, int64_t n, const double* x, double* out);
+// Generic permutation of a column-major tensor: out has dims in.dim[perm[k]].
+// out = alpha*permute(in) + beta*out
+void permute(tnad_ctx* c, const Ten& in, const int* perm, double* out, double alpha = 1.0,
+             double beta = 0.0);
+// Deterministic sum of squares into dev_out[0] (device).
+void sumsq_dev(tnad_ctx* c, const double* x, int64_t n, double* dev_out);
+// Σ x∘y into dev_out[0].
+void dot_dev(tnad_ctx* c, const double* x, const double* y, int64_t n, double* dev_out);
+// Blocking helpers returning host values.
+double norm_host(tnad_ctx* c, const double* x, int64_t n);
+double dot_host(tnad_ctx* c, const double* x, const double* y, int64_t n);
+// max |x| and its first index: dev_out[0] = max, dev_out[1] = index (as double)
+void maxabs_dev(tnad_ctx* c, const double* x, int64_t n, double* dev_out);
+// x /= dev_s[0]
+void div_by_dev(tnad_ctx* c, double* x, int64_t n, const double* dev_s);
+// x = x * dev_s[0] ... generic scalar ops on device scalars
+void normalize_inplace(tnad_ctx* c, double* x, int64_t n, double* dev_norm_out);
+
+// ---------------- GEMM (gemm_f64.cu, gemm_tc.cu) ----------------
+// Column-major C(M×N) = alpha·op(A)·op(B) + beta·C ; ta/tb in {'N','T'}.
+void gemm_f64(tnad_ctx* c, char ta, char tb, int64_t M, int64_t N, int64_t K, double alpha,
+              const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C,
+              int64_t ldc);
+// Same contract, 3xTF32 on tcgen05 tensor cores with FP32 accumulation.
+void gemm_tf32x3(tnad_ctx* c, char ta, char tb, int64_t M, int64_t N, int64_t K, double alpha,
+                 const double* A, int64_t lda, const double* B, int64_t ldb, double beta,
+                 double* C, int64_t ldc);
+void gemm(tnad_ctx* c, int prec, char ta, char tb, int64_t M, int64_t N, int64_t K, double alpha,
+          const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C,
+          int64_t ldc);
+
+// ---------------- pairwise contraction (contract.cpp) ----------------
+// C[lc] = alpha · Σ A[la]·B[lb] + beta·C[lc]; labels are single characters.
+// C.p must hold numel(C); its dims are filled in from A and B.
+void contract(tnad_ctx* c, int prec, const Ten& A, const char* la, const Ten& B, const char* lb,
+              Ten& C, const char* lc, double alpha = 1.0, double beta = 0.0);
+// Output dims of a contraction (without computing).
+Ten contract_shape(const Ten& A, const char* la, const Ten& B, const char* lb, const char* lc);
+
+// ---------------- FP64 Jacobi SVD (jacobi.cu) ----------------
+// Thin SVD of m×n (m ≥ n) A: U m×n, S n (descending), V n×n.  A is not modified.
+// symmetric=true: A is symmetric, null-space columns of U are completed from V.
+void svd_jacobi(tnad_ctx* c, const double* A, int64_t m, int64_t n, double* U, double* S,
+                double* V, bool symmetric);
+// Symmetric eigendecomposition of a small p×p matrix (p ≤ 256) by cyclic Jacobi in
+// one CTA: A = W·diag(lam)·Wᵀ, sorted by |lam| descending.
+void eigh_small(tnad_ctx* c, const double* A, int64_t p, double* W, double* lam);
+
+// ---------------- SVD adjoint (svd_back.cu) ----------------
+// svd_back for thin SVD (U m×n, S n, V n×n), dU m×n or null, dS n or null, dV n×n or null.
+void svd_back(tnad_ctx* c, int prec, const double* U, const double* S, const double* V, int64_t m,
+              int64_t n, const double* dU, const double* dS, const double* dV, double eta,
+              double* dA);
+
+}  // namespace tnad

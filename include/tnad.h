@@ -175,6 +175,13 @@ int tnad_energy(tnad_ctx* ctx, const double* h, const double* A, int D, int s, i
                 tnad_tape** tape);
 /* dA = dE · ∂energy/∂A (Zygote.gradient of energy, src/variationalipeps.jl:71-73). */
 int tnad_energy_backward(tnad_ctx* ctx, tnad_tape* tape, double dE, double* dA);
+/* Diagnostics of an energy tape (any pointer may be NULL): CTMRG steps, FP64
+   polishing steps of the mixed solver, step of the TF32X3→FP64 hand-over,
+   fixed-point adjoint iterations (after tnad_energy_backward), last stop-rule
+   residual and last fixed-point relative residual.  No reference counterpart
+   (the reference reports none of these). */
+int tnad_energy_stats(const tnad_tape* tape, int* steps, int* fp64_steps, int* switch_step, int* fp_iters,
+                      double* last_diff, double* fp_residual);
 
 #ifdef __cplusplus
 }

@@ -373,14 +373,34 @@ def energy(h, ipeps, chi: int, tol: float, maxit: int, opts=None) -> float:
     return _energy(h, ipeps, chi, tol, maxit, opts).E
 
 
-def energy_and_gradient(h, ipeps, chi: int, tol: float, maxit: int, opts=None, env=None):
-    """(E, ∂E/∂bulk): Zygote.gradient of energy (src/variationalipeps.jl:71-73)."""
+def energy_and_gradient(h, ipeps, chi: int, tol: float, maxit: int, opts=None, env=None, stats: dict | None = None):
+    """(E, ∂E/∂bulk): Zygote.gradient of energy (src/variationalipeps.jl:71-73).
+
+    ``stats`` (optional dict) receives the solver diagnostics of tnad_energy_stats."""
     r = _energy(h, ipeps, chi, tol, maxit, opts, record=True, env=env)
     bulk = ipeps.bulk if isinstance(ipeps, IPEPS) else farr(ipeps)
     g = fzeros(bulk.shape)
     c = r.tape.c
     c.check(c.lib.tnad_energy_backward(c.h, r.tape.h, 1.0, ptr(g)))
+    if stats is not None:
+        stats.update(tape_stats(r.tape))
     return r.E, g
+
+
+def tape_stats(tape) -> dict:
+    vals = [C.c_int() for _ in range(4)] + [C.c_double(), C.c_double()]
+    rc = tape.c.lib.tnad_energy_stats(tape.h, *[C.byref(v) for v in vals])
+    if rc != 0:
+        raise TnadError(rc, "tnad_energy_stats")
+    keys = ["steps", "fp64_steps", "switch_step", "fp_iters", "last_diff", "fp_residual"]
+    return {k: v.value for k, v in zip(keys, vals)}
+
+
+def mixed_opts(ladder_tol: float = 1e-5, fp_tol: float = 1e-9, fp_maxit: int = 200, **kw) -> L.Opts:
+    """Options of the mixed path: TF32X3 contractions with the FP64 polishing ladder,
+    the warm-started subspace solver, and the implicit fixed-point adjoint."""
+    return default_opts(prec=L.PREC_LADDER, solver=L.SOLVER_SUBSPACE, adjoint=L.ADJOINT_FIXEDPOINT, stop_rule=1,
+                        ladder_tol=ladder_tol, fp_tol=fp_tol, fp_maxit=fp_maxit, **kw)
 
 
 def optimiseipeps(ipeps: IPEPS, h, chi: int, tol: float, maxit: int, f_tol: float = 1e-6, iterations: int = 1000,

@@ -79,6 +79,7 @@ SIGNATURES = {
     "tnad_energy": (C.c_int, [VP, DP, DP, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.POINTER(Opts), DP, DP,
                               DP, IP, DP, DP, C.POINTER(VP)]),
     "tnad_energy_backward": (C.c_int, [VP, VP, C.c_double, DP]),
+    "tnad_energy_stats": (C.c_int, [VP, IP, IP, IP, IP, DP, DP]),
 }
 
 _lib = None

@@ -42,6 +42,7 @@ void to_host(tnad_ctx* c, double* out, const double* d, int64_t n, bool dev) {
 void finish_call(tnad_ctx* c) {
   TNAD_CK(cudaStreamSynchronize(c->stream));
   TNAD_CK(cudaGetLastError());
+  check_tc_errors(c);
 }
 
 tnad_opts opts_or_default(const tnad_opts* o) {
@@ -435,4 +436,17 @@ extern "C" int tnad_energy_backward(tnad_ctx* c, tnad_tape* tape, double dE, dou
   to_host(c, dA, g, nA, tape->dev);
   finish_call(c);
   API_END(c)
+}
+
+extern "C" int tnad_energy_stats(const tnad_tape* t, int* steps, int* fp64_steps, int* switch_step, int* fp_iters,
+                                 double* last_diff, double* fp_residual) {
+  if (!t || t->kind != 3 || !t->en) return TNAD_ERR_STATE;
+  const EnergyTape& e = *t->en;
+  if (steps) *steps = e.steps;
+  if (fp64_steps) *fp64_steps = e.fp64_steps;
+  if (switch_step) *switch_step = e.switch_step;
+  if (fp_iters) *fp_iters = e.fp_iters;
+  if (last_diff) *last_diff = e.last_diff;
+  if (fp_residual) *fp_residual = e.fp_residual;
+  return TNAD_OK;
 }

@@ -88,17 +88,19 @@ __global__ void k_norm_bwd(int64_t n, const double* __restrict__ dy, const doubl
 
 static int nb(int64_t n) { return (int)std::min<int64_t>((n + 255) / 256, 4096); }
 
+// S = (B − Bᵀ)/2 for an m×m B
+__global__ void k_skew(const double* __restrict__ B, int m, double* __restrict__ S) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < m * m; e += gridDim.x * blockDim.x) {
+    const int i = e % m, j = e / m;
+    S[e] = 0.5 * (B[i + j * m] - B[j + i * m]);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // forward step
 // ---------------------------------------------------------------------------
-struct StepFwd {
-  Ten X1, X2, cp, w, y1, y2, Cn, Tn;
-  double *M = nullptr, *Cs = nullptr, *Ts = nullptr;
-  double *nC = nullptr, *nT = nullptr;  // device scalars
-};
-
 // cp = ein"ad,iba,dcl,jkcb -> ijlk"(corner, edge, edge, bulk)  (src/ctmrg.jl:130)
-static void grow(tnad_ctx* c, int prec, const Ten& a, const Ten& C, const Ten& T, StepFwd& f) {
+void grow(tnad_ctx* c, int prec, const Ten& a, const Ten& C, const Ten& T, StepFwd& f) {
   int64_t chi = C.dim[0], d = a.dim[0];
   f.X1.p = ws_d(c, chi * d * chi);
   contract(c, prec, T, "iba", C, "ad", f.X1, "ibd");
@@ -110,7 +112,7 @@ static void grow(tnad_ctx* c, int prec, const Ten& a, const Ten& C, const Ten& T
 
 // corner = ein"abcd,abi,cdj -> ij"(cp, z, z); edge = ein"abjcd,abi,dck -> ijk"(tp, z, z)
 // with tp = ein"iam,jkla -> ijklm"(edge, bulk) never materialised (src/ctmrg.jl:131,139-140).
-static void project(tnad_ctx* c, int prec, const Ten& a, const Ten& T, const Ten& z, StepFwd& f) {
+void project(tnad_ctx* c, int prec, const Ten& a, const Ten& T, const Ten& z, StepFwd& f) {
   int64_t chi = T.dim[0], d = a.dim[0];
   f.w.p = ws_d(c, chi * chi * d);
   contract(c, prec, f.cp, "abcd", z, "abi", f.w, "icd");
@@ -125,7 +127,7 @@ static void project(tnad_ctx* c, int prec, const Ten& a, const Ten& T, const Ten
 }
 
 // symmetrise + normalise (src/ctmrg.jl:145-150) into Cout/Tout
-static void finish(tnad_ctx* c, int64_t chi, int64_t d, StepFwd& f, double* Cout, double* Tout) {
+void finish(tnad_ctx* c, int64_t chi, int64_t d, StepFwd& f, double* Cout, double* Tout) {
   f.Cs = ws_d(c, chi * chi);
   f.Ts = ws_d(c, chi * d * chi);
   add_transpose(c, chi, f.Cn.p, f.Cs);
@@ -166,14 +168,20 @@ void ctmrg_step_fwd(tnad_ctx* c, int prec, const double* a_, int d, int chi, con
 // ---------------------------------------------------------------------------
 void ctmrg_step_bwd(tnad_ctx* c, int prec, const double* a_, int d, int chi, const double* C_, const double* T_,
                     const double* U, const double* S, const double* V, const double* dCn_, const double* dTn_,
-                    double* dbulk, double* dC, double* dT, bool accumulate_bulk) {
+                    double* dbulk, double* dC, double* dT, bool accumulate_bulk, const double* O,
+                    const double* zref) {
   WsScope scope(c);
   const int64_t n = (int64_t)chi * d;
   const int64_t nCh = (int64_t)chi * chi, nTe = (int64_t)chi * d * chi;
   Ten a = make_ten(const_cast<double*>(a_), {d, d, d, d});
   Ten C = make_ten(const_cast<double*>(C_), {chi, chi});
   Ten T = make_ten(const_cast<double*>(T_), {chi, d, chi});
+  // z = U[:, 1:χ], or U[:, 1:χ]·O for a gauge-rotated projector (O χ×χ orthogonal)
   Ten z = make_ten(const_cast<double*>(U), {chi, d, chi});
+  if (O) {
+    z.p = ws_d(c, n * chi);
+    gemm(c, prec, 'N', 'N', n, chi, chi, 1.0, U, n, O, chi, 0.0, z.p, n);
+  }
   // recompute the forward intermediates (the decomposition comes from the tape)
   StepFwd f;
   grow(c, prec, a, C, T, f);
@@ -224,7 +232,23 @@ void ctmrg_step_bwd(tnad_ctx* c, int prec, const double* a_, int d, int chi, con
   // svd pullback with dU = [dz, 0]  (only u is used downstream: src/ctmrg.jl:137)
   double* dUfull = ws_d(c, n * n);
   fill(c, dUfull, n * n, 0.0);
-  copy_d2d(c, dUfull, dz.p, n * chi);
+  if (O) {
+    // z = U_χ·O(U_χ) with O = polar(U_χᵀ·R), R = zref held fixed.  Pullback of
+    // the polar factor at X ≈ O:  Ū_χ = (z̄ − R·skew(zᵀ·z̄))·Oᵀ, which makes
+    // U_χᵀ·Ū_χ symmetric: rotations inside the kept subspace (pure gauge) carry
+    // no cotangent, so their 1/(λ_i − λ_j) factors in svd_back never act.
+    double* B = ws_d(c, (int64_t)chi * chi);
+    double* Sk = ws_d(c, (int64_t)chi * chi);
+    double* dz2 = ws_d(c, n * chi);
+    gemm_f64(c, 'T', 'N', chi, chi, n, 1.0, z.p, n, dz.p, n, 0.0, B, chi);
+    k_skew<<<nb((int64_t)chi * chi), 256, 0, c->stream>>>(B, chi, Sk);
+    count_launch(c);
+    copy_d2d(c, dz2, dz.p, n * chi);
+    gemm(c, prec, 'N', 'N', n, chi, chi, -1.0, zref, n, Sk, chi, 1.0, dz2, n);
+    gemm(c, prec, 'N', 'T', n, chi, chi, 1.0, dz2, n, O, chi, 0.0, dUfull, n);
+  } else {
+    copy_d2d(c, dUfull, dz.p, n * chi);
+  }
   double* dM = ws_d(c, n * n);
   svd_back(c, prec, U, S, V, n, n, dUfull, nullptr, nullptr, 1e-40, dM);
   // cpmat += cpmat'  →  dcp += dM + dMᵀ

@@ -1,0 +1,324 @@
+// Small dense kernels of the subspace eigensolver, each in one CTA:
+//  - Cholesky of a p×p Gram matrix and the inverse of its triangular factor
+//    (CholeskyQR of the n×p block: Q = Y·R⁻¹);
+//  - cyclic parallel Jacobi eigendecomposition of a symmetric p×p matrix held
+//    in shared memory (circle-method rounds of p/2 disjoint rotations), in
+//    FP32 while the contractions run at 3xTF32 accuracy and in FP64 for the
+//    polishing steps; eigenvectors accumulate in global memory;
+//  - a counter-based Gaussian generator for deterministic start blocks.
+#include <cfloat>
+#include <cmath>
+
+#include "tnad_internal.h"
+
+namespace tnad {
+
+// ---------------------------------------------------------------- Cholesky
+// G (p×p, column-major, symmetric positive definite) → Rinv (p×p) with
+// G = RᵀR, R upper triangular.  *fail = 1 when a pivot is not positive.
+__global__ void k_chol_inv(const double* __restrict__ G, int p, double* __restrict__ Rinv, int* __restrict__ fail) {
+  extern __shared__ double sm[];
+  double* R = sm;  // p×p, column-major, upper triangle used
+  for (int e = threadIdx.x; e < p * p; e += blockDim.x) R[e] = G[e];
+  __syncthreads();
+  __shared__ int bad;
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  // right-looking: for k, R[k,k] = sqrt(R[k,k]); R[k,j] /= R[k,k] (j>k); trailing update
+  for (int k = 0; k < p; ++k) {
+    if (threadIdx.x == 0) {
+      double d = R[k + k * p];
+      if (!(d > 0.0)) {
+        bad = 1;
+        d = 1e-300;
+      }
+      R[k + k * p] = sqrt(d);
+    }
+    __syncthreads();
+    const double rkk = R[k + k * p];
+    for (int j = k + 1 + threadIdx.x; j < p; j += blockDim.x) R[k + j * p] /= rkk;
+    __syncthreads();
+    // trailing update of the upper triangle: R[i,j] -= R[k,i]·R[k,j] for k<i<=j
+    const int m = p - k - 1;
+    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+      const int i = k + 1 + e % m, j = k + 1 + e / m;
+      if (i <= j) R[i + j * p] -= R[k + i * p] * R[k + j * p];
+    }
+    __syncthreads();
+  }
+  // inverse of the upper-triangular R: column j of X solves R·x = e_j (back substitution)
+  for (int j = threadIdx.x; j < p; j += blockDim.x) {
+    for (int i = p - 1; i >= 0; --i) {
+      double s = (i == j) ? 1.0 : 0.0;
+      for (int l = i + 1; l <= j; ++l) s -= R[i + l * p] * Rinv[l + (int64_t)j * p];
+      Rinv[i + (int64_t)j * p] = (i <= j) ? s / R[i + i * p] : 0.0;
+    }
+  }
+  if (threadIdx.x == 0 && bad) *fail = 1;
+}
+
+void chol_inv_upper(tnad_ctx* c, const double* G, int64_t p, double* Rinv, int* dev_fail) {
+  TNAD_REQUIRE(p >= 1 && p <= 160, TNAD_ERR_SHAPE, "chol_inv_upper: p must be in [1,160]");
+  size_t sm = (size_t)p * p * 8;
+  static bool attr = false;
+  if (!attr) {
+    TNAD_CK(cudaFuncSetAttribute(k_chol_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 160 * 8));
+    attr = true;
+  }
+  k_chol_inv<<<1, 256, sm, c->stream>>>(G, (int)p, Rinv, dev_fail);
+  count_launch(c);
+  check_launch(c, "chol_inv");
+}
+
+// ---------------------------------------------------------------- Jacobi eigh
+__device__ __forceinline__ void circle_pair(int r, int k, int NP, int* p, int* q) {
+  if (k == 0) {
+    *p = NP - 1;
+    *q = r;
+  } else {
+    *p = (r + k) % (NP - 1);
+    *q = (r - k + (NP - 1)) % (NP - 1);
+  }
+}
+
+// A (p×p symmetric, FP64 in global) → lam (p, sorted by |λ| descending), W (p×p
+// eigenvectors as columns, same order).  Wtmp: p×p scratch for the unsorted
+// vectors.  Sweeps until no rotation is needed (or max_sweeps; *nsweeps out).
+template <typename T>
+__global__ void k_eigh_jacobi(const double* __restrict__ A, int p, int max_sweeps, double* __restrict__ lam,
+                              double* __restrict__ W, T* __restrict__ Z, int* __restrict__ info) {
+  extern __shared__ unsigned char smraw[];
+  T* H = reinterpret_cast<T*>(smraw);  // p×p
+  __shared__ T cs_[128], sn_[128];
+  __shared__ int pp_[128], qq_[128];
+  __shared__ int rotated;
+  const int NP = p + (p & 1);
+  const T tol = (T)(sizeof(T) == 8 ? 4.0 * DBL_EPSILON : 4.0 * FLT_EPSILON) * (T)sqrt((double)p);
+  for (int e = threadIdx.x; e < p * p; e += blockDim.x) {
+    H[e] = (T)A[e];
+    Z[e] = (e % p == e / p) ? (T)1 : (T)0;
+  }
+  __syncthreads();
+  int sweep = 0;
+  for (; sweep < max_sweeps; ++sweep) {
+    if (threadIdx.x == 0) rotated = 0;
+    __syncthreads();
+    for (int r = 0; r < NP - 1; ++r) {
+      // rotation parameters for the NP/2 disjoint pairs of this round
+      for (int k = threadIdx.x; k < NP / 2; k += blockDim.x) {
+        int a, b;
+        circle_pair(r, k, NP, &a, &b);
+        T c = 1, s = 0;
+        if (a < p && b < p) {
+          if (a > b) {
+            int t = a;
+            a = b;
+            b = t;
+          }
+          const T apq = H[a + b * p], app = H[a + a * p], aqq = H[b + b * p];
+          if (apq != (T)0 && fabs((double)apq) > (double)tol * sqrt(fabs((double)app * (double)aqq)) &&
+              fabs((double)apq) > 1e-300) {
+            const T tau = (aqq - app) / ((T)2 * apq);
+            const T t = (tau >= (T)0 ? (T)1 : (T)-1) / (fabs(tau) + sqrt((T)1 + tau * tau));
+            c = (T)1 / sqrt((T)1 + t * t);
+            s = t * c;
+            rotated = 1;
+          }
+        } else {
+          a = b = -1;
+        }
+        pp_[k] = a;
+        qq_[k] = b;
+        cs_[k] = c;
+        sn_[k] = s;
+      }
+      __syncthreads();
+      // rows: (row a, row b) ← (c·row a − s·row b, s·row a + c·row b)
+      for (int e = threadIdx.x; e < (NP / 2) * p; e += blockDim.x) {
+        const int k = e / p, col = e % p;
+        const int a = pp_[k], b = qq_[k];
+        if (a < 0 || sn_[k] == (T)0) continue;
+        const T c = cs_[k], s = sn_[k];
+        const T x = H[a + col * p], y = H[b + col * p];
+        H[a + col * p] = c * x - s * y;
+        H[b + col * p] = s * x + c * y;
+      }
+      __syncthreads();
+      // columns of H and of Z
+      for (int e = threadIdx.x; e < (NP / 2) * p; e += blockDim.x) {
+        const int k = e / p, row = e % p;
+        const int a = pp_[k], b = qq_[k];
+        if (a < 0 || sn_[k] == (T)0) continue;
+        const T c = cs_[k], s = sn_[k];
+        const T x = H[row + a * p], y = H[row + b * p];
+        H[row + a * p] = c * x - s * y;
+        H[row + b * p] = s * x + c * y;
+        const T zx = Z[row + a * p], zy = Z[row + b * p];
+        Z[row + a * p] = c * zx - s * zy;
+        Z[row + b * p] = s * zx + c * zy;
+      }
+      __syncthreads();
+      for (int k = threadIdx.x; k < NP / 2; k += blockDim.x) {
+        const int a = pp_[k], b = qq_[k];
+        if (a >= 0 && sn_[k] != (T)0) {
+          H[a + b * p] = (T)0;
+          H[b + a * p] = (T)0;
+        }
+      }
+      __syncthreads();
+    }
+    const int done = (rotated == 0);
+    __syncthreads();
+    if (done) break;
+  }
+  // sort by |λ| descending (ties by index): rank_j = #{i: |λ_i| > |λ_j| or (= and i<j)}
+  for (int j = threadIdx.x; j < p; j += blockDim.x) {
+    const double lj = (double)H[j + j * p];
+    int rk = 0;
+    for (int i = 0; i < p; ++i) {
+      const double li = (double)H[i + i * p];
+      rk += (fabs(li) > fabs(lj) || (fabs(li) == fabs(lj) && i < j)) ? 1 : 0;
+    }
+    lam[rk] = lj;
+    for (int i = 0; i < p; ++i) W[i + (int64_t)rk * p] = (double)Z[i + (int64_t)j * p];
+  }
+  if (threadIdx.x == 0 && info) info[0] = sweep;
+}
+
+void eigh_small_prec(tnad_ctx* c, bool fp32, const double* A, int64_t p, double* W, double* lam, int max_sweeps,
+                     int* dev_info) {
+  TNAD_REQUIRE(p >= 1 && p <= 256, TNAD_ERR_SHAPE, "eigh_small: p must be in [1,256]");
+  WsScope scope(c);
+  size_t sm = (size_t)p * p * (fp32 ? 4 : 8);
+  TNAD_REQUIRE(sm <= 200 * 1024, TNAD_ERR_SHAPE, "eigh_small: matrix does not fit in shared memory");
+  static bool attr32 = false, attr64 = false;
+  if (fp32) {
+    if (!attr32) {
+      TNAD_CK(cudaFuncSetAttribute(k_eigh_jacobi<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+      attr32 = true;
+    }
+    float* Z = ws_f(c, p * p);
+    k_eigh_jacobi<float><<<1, 512, sm, c->stream>>>(A, (int)p, max_sweeps, lam, W, Z, dev_info);
+  } else {
+    if (!attr64) {
+      TNAD_CK(cudaFuncSetAttribute(k_eigh_jacobi<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+      attr64 = true;
+    }
+    double* Z = ws_d(c, p * p);
+    k_eigh_jacobi<double><<<1, 512, sm, c->stream>>>(A, (int)p, max_sweeps, lam, W, Z, dev_info);
+  }
+  count_launch(c);
+  check_launch(c, "eigh_small");
+}
+
+void eigh_small(tnad_ctx* c, const double* A, int64_t p, double* W, double* lam) {
+  eigh_small_prec(c, false, A, p, W, lam, 40, nullptr);
+}
+
+// ---------------------------------------------------------------- polar factor
+// O = polar(X) for a χ×χ X (χ ≤ 128) by Newton–Schulz, O ← O·(3I − OᵀO)/2,
+// in FP32 in one CTA (the caller polishes in FP64).  info[0] = 1 when the
+// result is orthogonal to 1e-4 (else the caller falls back to sign alignment).
+__global__ void k_polar_ns(const double* __restrict__ X, int m, int iters, double* __restrict__ O,
+                           int* __restrict__ info) {
+  extern __shared__ float psm[];
+  float* A = psm;          // m×m current iterate
+  float* G = psm + m * m;  // m×m scratch
+  __shared__ float red[32];
+  const int mm = m * m;
+  // scale by 1/‖X‖_F·√m so that all singular values are ≤ 1 < √3
+  float s = 0.f;
+  for (int e = threadIdx.x; e < mm; e += blockDim.x) s += (float)(X[e] * X[e]);
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = 0.f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    red[0] = t > 0.f ? sqrtf((float)m / t) : 1.f;
+  }
+  __syncthreads();
+  const float sc = fminf(red[0], 1.0f) * 0.999f;
+  for (int e = threadIdx.x; e < mm; e += blockDim.x) A[e] = (float)X[e] * (red[0] > 1.f ? sc : 1.0f);
+  __syncthreads();
+  for (int it = 0; it < iters; ++it) {
+    // G = AᵀA
+    for (int e = threadIdx.x; e < mm; e += blockDim.x) {
+      const int i = e % m, j = e / m;
+      float acc = 0.f;
+      for (int k = 0; k < m; ++k) acc += A[k + i * m] * A[k + j * m];
+      G[e] = acc;
+    }
+    __syncthreads();
+    // A ← A·(1.5 I − 0.5 G)   (row i of A times G; one thread per element, into O as scratch)
+    for (int e = threadIdx.x; e < mm; e += blockDim.x) {
+      const int i = e % m, j = e / m;
+      float acc = 1.5f * A[i + j * m];
+      for (int k = 0; k < m; ++k) acc -= 0.5f * A[i + k * m] * G[k + j * m];
+      O[e] = (double)acc;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < mm; e += blockDim.x) A[e] = (float)O[e];
+    __syncthreads();
+  }
+  // orthogonality check
+  float worst = 0.f;
+  for (int e = threadIdx.x; e < mm; e += blockDim.x) {
+    const int i = e % m, j = e / m;
+    float acc = 0.f;
+    for (int k = 0; k < m; ++k) acc += A[k + i * m] * A[k + j * m];
+    worst = fmaxf(worst, fabsf(acc - (i == j ? 1.f : 0.f)));
+  }
+  for (int o = 16; o > 0; o >>= 1) worst = fmaxf(worst, __shfl_xor_sync(0xffffffffu, worst, o));
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = worst;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = 0.f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t = fmaxf(t, red[w]);
+    info[0] = t < 1e-4f ? 1 : 0;
+  }
+}
+
+void polar_ns(tnad_ctx* c, const double* X, int64_t m, int iters, double* O, int* dev_info) {
+  TNAD_REQUIRE(m >= 1 && m <= 128, TNAD_ERR_SHAPE, "polar_ns: m must be in [1,128]");
+  static bool attr = false;
+  if (!attr) {
+    TNAD_CK(cudaFuncSetAttribute(k_polar_ns, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 128 * 128 * 4));
+    attr = true;
+  }
+  k_polar_ns<<<1, 1024, (size_t)2 * m * m * 4, c->stream>>>(X, (int)m, iters, O, dev_info);
+  count_launch(c);
+  check_launch(c, "polar_ns");
+}
+
+// ---------------------------------------------------------------- Gaussian fill
+__device__ __forceinline__ uint64_t mix64(uint64_t x) {
+  x ^= x >> 30;
+  x *= 0xbf58476d1ce4e5b9ull;
+  x ^= x >> 27;
+  x *= 0x94d049bb133111ebull;
+  x ^= x >> 31;
+  return x;
+}
+
+// x[i] = scale·N(0,1) sample from a counter-based hash (SplitMix64 finaliser + Box–Muller)
+__global__ void k_randn(double* __restrict__ x, int64_t n, uint64_t seed, double scale, int accumulate) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t h1 = mix64(seed * 0x9e3779b97f4a7c15ull + 2 * (uint64_t)i + 1);
+    const uint64_t h2 = mix64(h1 ^ 0xd6e8feb86659fd93ull);
+    const double u1 = ((double)(h1 >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+    const double u2 = (double)(h2 >> 11) * (1.0 / 9007199254740992.0);
+    const double g = sqrt(-2.0 * log(u1)) * cospi(2.0 * u2);
+    x[i] = accumulate ? x[i] + scale * g : scale * g;
+  }
+}
+
+void randn(tnad_ctx* c, double* x, int64_t n, uint64_t seed, double scale, bool accumulate) {
+  int nb = (int)std::min<int64_t>((n + 255) / 256, 4096);
+  k_randn<<<nb, 256, 0, c->stream>>>(x, n, seed, scale, accumulate ? 1 : 0);
+  count_launch(c);
+  check_launch(c, "randn");
+}
+
+}  // namespace tnad

@@ -5,6 +5,7 @@
 #include <cmath>
 
 #include "tnad_energy.h"
+#include "tnad_mixed.h"
 
 namespace tnad {
 
@@ -254,9 +255,34 @@ void energy_fwd(tnad_ctx* c, EnergyTape& tp, const double* h, const double* A, i
   } else {
     init_raw_dev(c, tp.a, d, chi, tp.C, tp.T);
   }
-  CtmrgRun run = ctmrg_run(c, o.prec == TNAD_PREC_FP64 ? TNAD_PREC_FP64 : TNAD_PREC_TF32X3, tp.a, d, chi, tp.C, tp.T,
-                           tol, maxit, record ? &tp.ct : nullptr, &P, o.tape_budget);
-  tp.steps = run.steps;
+  tp.solver = o.solver;
+  tp.adjoint = o.adjoint;
+  tp.fp_tol = o.fp_tol;
+  tp.fp_maxit = o.fp_maxit;
+  const int64_t n = (int64_t)chi * d;
+  if (o.solver == TNAD_SOLVER_SUBSPACE) {
+    // mixed precision + subspace solver; the implicit adjoint needs only x* and z*
+    if (record) tp.zstar = P.d(n * chi);
+    MixedRun run = ctmrg_run_mixed(c, tp.a, d, chi, tp.C, tp.T, tol, maxit, o, record ? tp.zstar : nullptr);
+    tp.steps = run.steps;
+    tp.fp64_steps = run.fp64_steps;
+    tp.switch_step = run.switch_step;
+    tp.last_diff = run.last_diff;
+    TNAD_REQUIRE(!record || o.adjoint == TNAD_ADJOINT_FIXEDPOINT, TNAD_ERR_ARG,
+                 "energy: the subspace solver is differentiated with the fixed-point adjoint only");
+  } else {
+    const bool full_tape = record && o.adjoint == TNAD_ADJOINT_UNROLLED;
+    CtmrgRun run = ctmrg_run(c, o.prec == TNAD_PREC_FP64 ? TNAD_PREC_FP64 : TNAD_PREC_TF32X3, tp.a, d, chi, tp.C,
+                             tp.T, tol, maxit, (full_tape || record) ? &tp.ct : nullptr, &P,
+                             full_tape ? o.tape_budget : (int64_t)(2 * n * n + n) * 8 * (maxit + 2));
+    tp.steps = run.steps;
+    tp.last_diff = run.last_diff;
+    if (record && o.adjoint == TNAD_ADJOINT_FIXEDPOINT) {
+      TNAD_REQUIRE(!tp.ct.U.empty() && tp.ct.U.back(), TNAD_ERR_STATE, "energy: missing last projector");
+      tp.zstar = P.d(n * chi);
+      copy_d2d(c, tp.zstar, tp.ct.U.back(), n * chi);
+    }
+  }
   WsScope scope(c);
   Expect x;
   expect_fwd(c, TNAD_PREC_FP64, tp.h, tp.ap, d, s, chi, tp.C, tp.T, x);
@@ -279,7 +305,15 @@ void energy_bwd(tnad_ctx* c, EnergyTape& tp, double dE, double* dA) {
   expect_bwd(c, TNAD_PREC_FP64, tp.h, d, s, chi, tp.C, tp.T, x, dE, dap, dC, dT);
   double* dbulk = ws_d(c, d4);
   fill(c, dbulk, d4, 0.0);
-  ctmrg_reverse(c, tp.ct, dC, dT, dbulk);
+  if (tp.adjoint == TNAD_ADJOINT_FIXEDPOINT) {
+    const int pr = tp.prec == TNAD_PREC_FP64 ? TNAD_PREC_FP64 : TNAD_PREC_TF32X3;
+    FixedPointInfo fi =
+        ctmrg_fixedpoint_adjoint(c, pr, tp.a, d, chi, tp.C, tp.T, tp.zstar, dC, dT, dbulk, tp.fp_tol, tp.fp_maxit);
+    tp.fp_iters = fi.iters;
+    tp.fp_residual = fi.residual;
+  } else {
+    ctmrg_reverse(c, tp.ct, dC, dT, dbulk);
+  }
   double* dAs = ws_d(c, (int64_t)D * D * D * D * s);
   double_layer_bwd(c, TNAD_PREC_FP64, tp.As, D, s, dap, dbulk, dAs);
   symmetrize_bwd(c, tp.As, tp.nA, D, s, dAs, dA);

@@ -145,10 +145,12 @@ void gemm_f64(tnad_ctx* c, char ta, char tb, int64_t M, int64_t N, int64_t K, do
 
 void gemm(tnad_ctx* c, int prec, char ta, char tb, int64_t M, int64_t N, int64_t K, double alpha, const double* A,
           int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc) {
-  if (prec == TNAD_PREC_TF32X3 && c->tc_ok)
+  if (prec == TNAD_PREC_TF32X3) {
+    TNAD_REQUIRE(c->tc_ok, TNAD_ERR_STATE, "TF32X3 contractions need an sm_100-family GPU (tcgen05)");
     gemm_tf32x3(c, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
-  else
+  } else {
     gemm_f64(c, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+  }
 }
 
 }  // namespace tnad

@@ -259,11 +259,12 @@ void svd_jacobi(tnad_ctx* c, const double* A, int64_t m, int64_t n, double* U, d
   // columns forever.  m·ε still leaves U, V orthogonal far below 1e-10.
   const double tol = (double)std::max<int64_t>(m, 16) * DBL_EPSILON;
   const double abs_eps = 2.0 * DBL_EPSILON;
-  // General A: only exactly-null columns are rebuilt.  A tiny but non-zero
-  // column keeps U_j = W_j/s_j so that A·V_j = s_j·U_j holds exactly: trg_svd
-  // keeps one singular value at the rounding floor (its +1 quirk) and the
-  // √s pullback of that column needs a consistent triplet.
-  const double weak_rel = 0.0;
+  // General A: columns with s_j ≤ 1e-8·‖A‖_F carry rounding noise in their
+  // direction; they are re-orthonormalised so that U stays orthogonal.  The SVD
+  // adjoint only needs those columns to span the complement of the larger ones
+  // (its F-matrix is ≈ 1/s_p² across that gap), and callers that differentiate
+  // through √s of such a column (trg_svd's +1 quirk) zero its value first.
+  const double weak_rel = 1e-8;
   int* flag = c->d_flag;
   bool converged = (n == 1);
   const int threads = 256;

@@ -29,6 +29,19 @@ struct CtmrgRun {
   double last_diff = 0.0;
 };
 
+// Intermediates of one step (workspace-backed).
+struct StepFwd {
+  Ten X1, X2, cp, w, y1, y2, Cn, Tn;
+  double *M = nullptr, *Cs = nullptr, *Ts = nullptr;
+  double *nC = nullptr, *nT = nullptr;  // device scalars
+};
+// cp = ein"ad,iba,dcl,jkcb -> ijlk"(C, T, T, a)                 (src/ctmrg.jl:130)
+void grow(tnad_ctx* c, int prec, const Ten& a, const Ten& C, const Ten& T, StepFwd& f);
+// C' = zᵀ·cp·z and T' = ein"abjcd,abi,dck -> ijk"(tp, z, z)       (src/ctmrg.jl:139-140)
+void project(tnad_ctx* c, int prec, const Ten& a, const Ten& T, const Ten& z, StepFwd& f);
+// symmetrise + normalise into Cout/Tout                          (src/ctmrg.jl:145-150)
+void finish(tnad_ctx* c, int64_t chi, int64_t d, StepFwd& f, double* Cout, double* Tout);
+
 // One CTMRG step (src/ctmrg.jl:126-153) on device buffers.  U/S/V: n×n, n, n×n
 // buffers that receive the decomposition (may be workspace).
 void ctmrg_step_fwd(tnad_ctx* c, int prec, const double* a, int d, int chi, const double* C, const double* T,
@@ -36,7 +49,8 @@ void ctmrg_step_fwd(tnad_ctx* c, int prec, const double* a, int d, int chi, cons
 // Pullback of one step.  dbulk/dC/dT are ACCUMULATED into (beta = 1) when accumulate.
 void ctmrg_step_bwd(tnad_ctx* c, int prec, const double* a, int d, int chi, const double* C, const double* T,
                     const double* U, const double* S, const double* V, const double* dCn, const double* dTn,
-                    double* dbulk, double* dC, double* dT, bool accumulate_bulk);
+                    double* dbulk, double* dC, double* dT, bool accumulate_bulk, const double* O = nullptr,
+                    const double* zref = nullptr);
 // ctmrg loop with the reference stop rule; C/T hold the initial env on entry and
 // the result on exit.  With tape != null every step's input and decomposition
 // are recorded (pool owns the memory).

@@ -15,10 +15,16 @@ struct Expect {
 
 struct EnergyTape {
   int D = 0, s = 0, chi = 0, d = 0, steps = 0, prec = TNAD_PREC_FP64;
+  int solver = TNAD_SOLVER_FULL_SVD, adjoint = TNAD_ADJOINT_UNROLLED;
+  int fp64_steps = 0, switch_step = 0;  // mixed solver: FP64 polishing steps, ladder hand-over
+  int fp_iters = 0;                     // fixed-point adjoint iterations used
+  double fp_residual = 0.0, fp_tol = 1e-10, last_diff = 0.0;
+  int fp_maxit = 200;
   double E = 0.0;
   DevPool pool;
   double *h = nullptr, *As = nullptr, *nA = nullptr, *ap = nullptr, *a = nullptr;
   double *C = nullptr, *T = nullptr;  // converged environment
+  double* zstar = nullptr;            // projector of the last step (n×χ), fixed-point adjoint
   CtmrgTape ct;
 };
 

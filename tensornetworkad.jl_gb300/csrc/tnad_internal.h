@@ -134,6 +134,8 @@ void gemm_f64(tnad_ctx* c, char ta, char tb, int64_t M, int64_t N, int64_t K, do
 void gemm_tf32x3(tnad_ctx* c, char ta, char tb, int64_t M, int64_t N, int64_t K, double alpha,
                  const double* A, int64_t lda, const double* B, int64_t ldb, double beta,
                  double* C, int64_t ldc);
+// Raises TNAD_ERR_TIMEOUT if a tensor-core GEMM gave up on a bounded wait (syncs).
+void check_tc_errors(tnad_ctx* c);
 void gemm(tnad_ctx* c, int prec, char ta, char tb, int64_t M, int64_t N, int64_t K, double alpha,
           const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C,
           int64_t ldc);

@@ -126,6 +126,19 @@ void trg_svd_fwd(tnad_ctx* c, const double* t, const int64_t dd[4], int chi, dou
   int64_t cnt = 0;
   for (double x : hs) cnt += (x > tol) ? 1 : 0;
   s.k = std::min<int64_t>(std::min<int64_t>(cnt + 1, chi), s.ns);
+  // Values at the rounding floor (at or below tol, or below 64ε·s₁ where the
+  // solver's absolute accuracy ends) carry noise vectors; LAPACK reports them as
+  // ~1e-17..1e-15 with its own noise.  They are set to exactly 0: a kept noise
+  // column (the +1 quirk) then contributes u = v = 0 and no noise-amplified √s
+  // pullback (d√s/ds = 1/(2√s)); lnZ moves by less than the floor itself.
+  const double floor_s = std::max(tol, 64.0 * 2.220446049250313e-16 * (hs.empty() ? 0.0 : hs[0]));
+  bool any = false;
+  for (double& x : hs)
+    if (x <= floor_s && x != 0.0) {
+      x = 0.0;
+      any = true;
+    }
+  if (any) TNAD_CK(cudaMemcpyAsync(s.S, hs.data(), s.ns * 8, cudaMemcpyHostToDevice, c->stream));
   s.u = pool->d(s.m * s.k);
   s.v = pool->d(s.k * s.n);
   k_trg_split<<<nb(s.m * s.k + s.k * s.n), 256, 0, c->stream>>>(s.U, s.S, s.V, s.m, s.n, s.k, s.u, s.v);

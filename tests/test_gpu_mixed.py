@@ -1,0 +1,62 @@
+"""Mixed path: TF32X3 tensor-core contractions + subspace solver + FP64 ladder,
+differentiated by the implicit fixed-point adjoint.  Checked against the CPU
+oracle (FP64, unrolled Zygote-equivalent gradient) and the converged-energy
+fixtures of tests/golden/estar.json."""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+ESTAR = json.loads((Path(__file__).parent / "golden" / "estar.json").read_text())
+
+
+def rel(a, b):
+    a, b = np.asarray(a, dtype=float), np.asarray(b, dtype=float)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def test_mixed_energy_D2(tn, orc):
+    h = tn.hamiltonian(tn.Heisenberg())
+    A = orc.ipeps_uniform(2, 2, 11)
+    E = tn.energy(h, tn.SquareIPEPS(A), 12, 1e-10, 200, opts=tn.mixed_opts())
+    E_r = float(orc.energy(h, torch.as_tensor(A), 12, 1e-12, 300))
+    assert abs(E - E_r) < 1e-9
+
+
+def test_mixed_energy_and_fixedpoint_gradient_D3_chi36(tn, orc):
+    """cfg3: D=3, χ=36, tol 1e-10.  Gradient error against the oracle's unrolled
+    gradient is bounded by the 3xTF32 adjoint contractions (1e-5 relative)."""
+    h = tn.hamiltonian(tn.Heisenberg())
+    A = orc.ipeps_uniform(3, 2, 0)
+    st = {}
+    E, g = tn.energy_and_gradient(h, tn.SquareIPEPS(A), 36, 1e-10, 200, opts=tn.mixed_opts(), stats=st)
+    E_r, g_r, _ = orc.energy_and_grad(h, A, 36, 1e-10, 100)
+    assert abs(E - E_r) < 1e-9
+    assert rel(g, g_r) < 1e-5, st
+    assert st["fp_iters"] >= 1
+
+
+def test_plain_fixedpoint_adjoint_matches_unrolled(tn, orc):
+    h = tn.hamiltonian(tn.Heisenberg())
+    A = orc.ipeps_uniform(2, 2, 7)
+    o = tn.default_opts(adjoint=1, fp_tol=1e-12)
+    E, g = tn.energy_and_gradient(h, tn.SquareIPEPS(A), 10, 1e-12, 300, opts=o)
+    E_r, g_r, _ = orc.energy_and_grad(h, A, 10, 1e-12, 300)
+    assert abs(E - E_r) < 1e-10 * abs(E_r)
+    assert rel(g, g_r) < 1e-7
+
+
+@pytest.mark.parametrize("name", ["heisenberg_D4_chi64"])
+def test_mixed_reaches_1e8_of_oracle_Estar(tn, orc, name):
+    """The headline target: |E − E*| ≤ 1e-8 at D=4, χ=64 on the mixed path."""
+    w = ESTAR[name]
+    A = orc.ipeps_normal_maxabs(w["D"], 2, w["seed"])
+    h = tn.hamiltonian(tn.Heisenberg())
+    st = {}
+    E, g = tn.energy_and_gradient(h, tn.SquareIPEPS(A), w["chi"], 3e-8, 400, opts=tn.mixed_opts(), stats=st)
+    assert abs(E - w["E_star"]) <= 1e-8, (E, w["E_star"], st)
+    assert np.all(np.isfinite(g))

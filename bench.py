@@ -41,7 +41,9 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--workload", default="heisenberg_D4_chi64")
-    p.add_argument("--mode", default="plain", choices=["plain", "mixed"])
+    p.add_argument("--mode", default="mixed", choices=["plain", "mixed"])
+    p.add_argument("--no-plain", dest="no_plain", action="store_true", help="skip the plain FP64 comparison solve")
+    p.add_argument("--no-cpu-baseline", dest="no_cpu_baseline", action="store_true")
     return p.parse_args()
 
 
@@ -137,6 +139,72 @@ def barrier(dist):
 
 
 # ---------------------------------------------------------------------------
+PEAKS_PATH = ROOT / "MEASURED_PEAKS.json"
+FP64_NOMINAL_TFLOPS = 1.25  # GB300 FP64 (no measured FP64 figure exists for this machine)
+# dram__bytes_read.sum + dram__bytes_write.sum per launch of the dominant kernel,
+# from the ncu capture summarised in profiles/jacobi_round_D4_chi64.md
+JACOBI_ROUND_TRAFFIC_BYTES = None
+
+
+def peaks():
+    try:
+        return json.loads(PEAKS_PATH.read_text()), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class Solver:
+    """One workload solved through libtnad: device-resident (kernel-side number)
+    or through the public API with host arrays (end to end)."""
+
+    def __init__(self, tn, w, mode):
+        import ctypes as C
+        import torch
+
+        self.C, self.tn, self.w, self.mode = C, tn, w, mode
+        self.c = tn.ctx(int(os.environ.get("LOCAL_RANK", "0")))
+        self.A = workload_input(w)
+        self.h = tn.hamiltonian(tn.Heisenberg())
+        self.chi, self.D, self.s = w["chi"], w["D"], 2
+        if mode == "plain":
+            self.opts, self.tol, self.maxit = tn.default_opts(), plain_tol(w), 400
+        else:
+            self.opts, self.tol, self.maxit = tn.mixed_opts(), 3e-8, 400
+        self.A_d = torch.tensor(np.asarray(self.A).ravel(order="F"), dtype=torch.float64, device="cuda")
+        self.h_d = torch.tensor(np.asarray(self.h).ravel(order="F"), dtype=torch.float64, device="cuda")
+        self.g_d = torch.zeros_like(self.A_d)
+        self.opts_d = tn.default_opts(**{k: getattr(self.opts, k) for k, _ in self.opts._fields_})
+        self.opts_d.device_ptrs = 1
+
+    def device(self):
+        C, tn, c = self.C, self.tn, self.c
+        E, steps, tp = C.c_double(), C.c_int(), tn._lib.VP()
+        c.check(c.lib.tnad_energy(c.h, tn.ptr(self.h_d.data_ptr()), tn.ptr(self.A_d.data_ptr()), self.D, self.s,
+                                  self.chi, self.tol, self.maxit, C.byref(self.opts_d), tn.ptr(None), tn.ptr(None),
+                                  C.byref(E), C.byref(steps), tn.ptr(None), tn.ptr(None), C.byref(tp)))
+        c.check(c.lib.tnad_energy_backward(c.h, tp, 1.0, tn.ptr(self.g_d.data_ptr())))
+        st = self.tn.tape_stats(self.tn._lib.Tape(c, tp, "energy"))  # frees the tape
+        return E.value, st
+
+    def host(self):
+        st = {}
+        E, g = self.tn.energy_and_gradient(self.h, self.tn.SquareIPEPS(self.A), self.chi, self.tol, self.maxit,
+                                           self.opts, stats=st)
+        return E, g, st
+
+
+def kernel_timer(c, name):
+    c.check(c.lib.tnad_ctx_kernel_timer(c.h, name.encode()))
+
+
+def kernel_timer_read(c):
+    import ctypes as C
+
+    n, ms, work = C.c_int64(), C.c_double(), C.c_double()
+    c.check(c.lib.tnad_ctx_kernel_timer_read(c.h, C.byref(n), C.byref(ms), C.byref(work)))
+    return n.value, ms.value, work.value
+
+
 def run_gb300(args):
     import torch
     import __graft_entry__ as ge
@@ -145,91 +213,103 @@ def run_gb300(args):
     torch.cuda.set_device(local)
     dist, rank, world = dist_init(args.gpus)
     tn = ge.load_package()
-    c = tn.ctx(local)
     w = ESTAR[args.workload]
-    A = workload_input(w)
-    h = tn.hamiltonian(tn.Heisenberg())
-    chi, D, s = w["chi"], w["D"], 2
-    if args.mode == "plain":
-        opts = tn.default_opts()
-        tol, maxit = plain_tol(w), 400
-    else:
-        opts = tn.default_opts(prec=1, solver=1, adjoint=1, stop_rule=1)
-        tol, maxit = 1e-10, 400
-    # device-resident inputs for the kernel-side number
-    A_d = torch.tensor(np.asarray(A).ravel(order="F"), dtype=torch.float64, device="cuda")
-    h_d = torch.tensor(np.asarray(h).ravel(order="F"), dtype=torch.float64, device="cuda")
-    g_d = torch.zeros_like(A_d)
-    opts_d = tn.default_opts(**{k: getattr(opts, k) for k, _ in opts._fields_})
-    opts_d.device_ptrs = 1
-
-    import ctypes as C
-
-    def solve_device():
-        E, steps, tp = C.c_double(), C.c_int(), tn._lib.VP()
-        c.check(c.lib.tnad_energy(c.h, tn.ptr(h_d.data_ptr()), tn.ptr(A_d.data_ptr()), D, s, chi, tol, maxit,
-                                  C.byref(opts_d), tn.ptr(None), tn.ptr(None), C.byref(E), C.byref(steps),
-                                  tn.ptr(None), tn.ptr(None), C.byref(tp)))
-        c.check(c.lib.tnad_energy_backward(c.h, tp, 1.0, tn.ptr(g_d.data_ptr())))
-        c.lib.tnad_tape_free(tp)
-        return E.value, steps.value
-
-    def solve_host():
-        E, g = tn.energy_and_gradient(h, tn.SquareIPEPS(A), chi, tol, maxit, opts)
-        return E, g
-
+    sol = Solver(tn, w, args.mode)
+    c = sol.c
     for _ in range(args.warmup):
-        solve_device()
+        sol.device()
     torch.cuda.synchronize()
     barrier(dist)
+    # timed region: K solves with device-resident inputs; the dominant kernel's
+    # launches are bracketed by CUDA events on the library's stream
+    kernel_timer(c, "jacobi_round")
     l0 = c.launches
-    errs = []
+    errs, stats = [], []
     with Clocks(local) as clk:
         torch.cuda.synchronize()
         barrier(dist)
+        stream = torch.cuda.ExternalStream(c.lib.tnad_ctx_stream(c.h))
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        t0 = time.perf_counter()
-        ev0.record()
-        steps_used = []
+        ev0.record(stream)
         for _ in range(args.steps):
-            E, st = solve_device()
+            E, st = sol.device()
             errs.append(abs(E - w["E_star"]))
-            steps_used.append(st)
-        ev1.record()
+            stats.append(st)
+        ev1.record(stream)
         torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
         barrier(dist)
     launches = (c.launches - l0) // args.steps
-    # Every solve synchronises with the host (stop rule), so host wall time over the
-    # bracketed region and the event interval agree; report the event interval.
-    t_dev = ev0.elapsed_time(ev1) / 1e3 / args.steps
-    t_dev = max_over_ranks(dist, t_dev)
-    # end-to-end through the public API with host arrays
-    solve_host()
+    t_dev = max_over_ranks(dist, ev0.elapsed_time(ev1) / 1e3 / args.steps)
+    kn, kms, kwork = kernel_timer_read(c)
+    kernel_timer(c, "gemm_tf32x3")
+    sol.device()
+    tn_n, tn_ms, tn_work = kernel_timer_read(c)
+    kernel_timer(c, "")
+    # end to end through the public API with host (NumPy) arrays
+    sol.host()
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     for _ in range(args.steps):
-        E_h, g_h = solve_host()
-    t_e2e = (time.perf_counter() - t1) / args.steps
-    t_e2e = max_over_ranks(dist, t_e2e)
+        E_h, g_h, st_h = sol.host()
+    t_e2e = max_over_ranks(dist, (time.perf_counter() - t1) / args.steps)
+    # the plain FP64 GPU path (full Jacobi SVD each step, unrolled reverse), one solve
+    plain = None
+    if args.mode == "mixed" and not args.no_plain:
+        ps = Solver(tn, w, "plain")
+        t2 = time.perf_counter()
+        Ep, stp = ps.device()
+        torch.cuda.synchronize()
+        tp_ = time.perf_counter() - t2
+        plain = {"value": round(tp_, 4), "unit": "s", "ctmrg_steps": stp["steps"], "delta_E": abs(Ep - w["E_star"]),
+                 "steps": 1, "warmup": 0}
     if rank != 0:
         return
-    nA = int(np.asarray(A).size)
+    pk, pk_kind = peaks()
+    rounds = kn / max(args.steps, 1)
+    ach_fp64 = (kwork / (kms / 1e3)) / 1e12 if kms > 0 else None
+    ach_tc = (tn_work / (tn_ms / 1e3)) / 1e12 if tn_ms > 0 else None
+    tf32_peak = pk.get("bf16_tflops", 1900.0) / 2.0
+    nA = int(np.asarray(sol.A).size)
     line = {
-        "metric": "CTMRG energy+gradient time to |dE|<=1e-8 vs FP64 oracle (D=4, chi=64)",
+        "metric": "CTMRG energy+gradient time to |dE|<=1e-8 vs the FP64 oracle (Heisenberg iPEPS D=4, chi=64)",
         "value": round(t_dev, 6), "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(t_dev * 1e3, 3), "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.mode == "plain" else "tf32x3+f64",
-        "data": "synthetic (seeded N(0,1) site tensor, max-abs normalised, symmetrised)",
-        "config": {"workload": args.workload, "D": D, "chi": chi, "phys": s, "mode": args.mode, "tol": tol,
-                   "ctmrg_steps": steps_used[-1], "parallelism": f"replicas x{world}",
-                   "l2": "working set (< 200 MB) is L2/HBM resident; no flush: each solve is seconds long"},
+        "data": "synthetic: N(0,1) site tensor (NumPy seed 0), max-abs normalised, symmetrised",
+        "config": {"workload": args.workload, "D": sol.D, "chi": sol.chi, "phys": sol.s, "mode": args.mode,
+                   "stop_tol": sol.tol, "ctmrg_steps": stats[-1]["steps"], "fp64_steps": stats[-1]["fp64_steps"],
+                   "fixedpoint_iters": stats[-1]["fp_iters"], "parallelism": f"replicas x{world}",
+                   "l2": "no flush: each solve runs ~10^4 launches over a <300 MB working set (L2/HBM resident)"},
         "delta_E": max(errs), "E": E, "E_star": w["E_star"],
         "e2e": {"value": round(t_e2e, 6), "unit": "s", "h2d_bytes_per_step": 8 * (nA + 16),
                 "d2h_bytes_per_step": 8 * (nA + 1)},
         "gpu_launches": int(launches),
+        "roofline": {"kernel": "k_jacobi_round_cta (FP64 one-sided Jacobi round, full SVD of the 1024x1024 corner "
+                               "for the implicit adjoint)",
+                     "bound": "fp64", "achieved": round(ach_fp64, 4) if ach_fp64 else None,
+                     "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
+                     "frac": round(ach_fp64 / FP64_NOMINAL_TFLOPS, 4) if ach_fp64 else None,
+                     "peak_kind": "nominal (no FP64 figure in MEASURED_PEAKS.json)",
+                     "traffic": JACOBI_ROUND_TRAFFIC_BYTES, "launches_per_step": round(rounds, 1),
+                     "avg_launch_us": round(kms * 1e3 / kn, 3) if kn else None,
+                     "share_of_step": round(kms / 1e3 / args.steps / t_dev, 4) if kn else None},
+        "roofline_tensor": {"kernel": "k_gemm_tf32x3 (tcgen05 kind::tf32, 3 split products)", "bound": "tensor",
+                            "achieved_logical": round(ach_tc, 3) if ach_tc else None,
+                            "achieved_hw": round(3 * ach_tc, 3) if ach_tc else None,
+                            "peak": tf32_peak, "unit": "TFLOP/s",
+                            "frac": round(3 * ach_tc / tf32_peak, 4) if ach_tc else None,
+                            "peak_kind": f"{pk_kind} bf16 burst / 2 (dense TF32 rate)",
+                            "launches_per_step": tn_n, "avg_launch_us": round(tn_ms * 1e3 / tn_n, 3) if tn_n else None},
         "clocks": clk.summary(),
     }
+    if plain:
+        line["plain_fp64"] = plain
+        line["speedup_vs_plain_fp64"] = round(plain["value"] / t_dev, 2)
+    if not args.no_cpu_baseline:
+        cb, need = oracle_sample(w)
+        line["cpu_baseline"] = {"value": round(cb, 3), "unit": "s", "cores": torch.get_num_threads(), "kind": "port",
+                                "sample": f"oracle (torch-CPU FP64): 4 CTMRG steps forward + reverse, scaled to the "
+                                          f"{need} steps it needs for |dE|<=1e-8"}
     print(json.dumps(line), flush=True)
 
 

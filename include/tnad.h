@@ -94,6 +94,15 @@ void tnad_opts_default(tnad_opts* o);
 int64_t tnad_ctx_workspace_bytes(const tnad_ctx* ctx);
 /* Number of CUDA kernels the context has launched so far. */
 int64_t tnad_ctx_kernel_launches(const tnad_ctx* ctx);
+/* Kernel timer (measurement support, no reference counterpart): from now on
+   bracket every launch of kernel family `name` ("jacobi_round", "gemm_tf32x3",
+   "gemm_f64"; "" switches it off) with CUDA events on the context stream. */
+int tnad_ctx_kernel_timer(tnad_ctx* ctx, const char* name);
+/* Totals since the timer was set: launches, summed device time (ms) and the
+   summed algorithmic work of those launches (FP64-equivalent flops).  Syncs. */
+int tnad_ctx_kernel_timer_read(tnad_ctx* ctx, int64_t* launches, double* total_ms, double* work);
+/* The context's CUDA stream (cudaStream_t), for callers that time around it. */
+void* tnad_ctx_stream(tnad_ctx* ctx);
 void tnad_tape_free(tnad_tape* tape);
 
 /* -------- building blocks (the role OMEinsum plays in the reference) -------- */

@@ -57,6 +57,9 @@ SIGNATURES = {
     "tnad_opts_default": (None, [C.POINTER(Opts)]),
     "tnad_ctx_workspace_bytes": (C.c_int64, [VP]),
     "tnad_ctx_kernel_launches": (C.c_int64, [VP]),
+    "tnad_ctx_kernel_timer": (C.c_int, [VP, C.c_char_p]),
+    "tnad_ctx_kernel_timer_read": (C.c_int, [VP, C.POINTER(C.c_int64), DP, DP]),
+    "tnad_ctx_stream": (VP, [VP]),
     "tnad_tape_free": (None, [VP]),
     "tnad_gemm": (C.c_int, [VP, C.c_int, C.c_char, C.c_char, C.c_int64, C.c_int64, C.c_int64, C.c_double, DP,
                             C.c_int64, DP, C.c_int64, C.c_double, DP, C.c_int64]),

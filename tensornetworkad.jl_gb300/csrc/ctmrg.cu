@@ -166,29 +166,46 @@ void ctmrg_step_fwd(tnad_ctx* c, int prec, const double* a_, int d, int chi, con
 // ---------------------------------------------------------------------------
 // pullback of one step
 // ---------------------------------------------------------------------------
+void step_cache_fill(tnad_ctx* c, int prec, const double* a_, int d, int chi, const double* C_, const double* T_,
+                     const double* U, const double* O, StepCache& sc) {
+  const int64_t n = (int64_t)chi * d;
+  Ten a = make_ten(const_cast<double*>(a_), {d, d, d, d});
+  Ten C = make_ten(const_cast<double*>(C_), {chi, chi});
+  Ten T = make_ten(const_cast<double*>(T_), {chi, d, chi});
+  // z = U[:, 1:χ], or U[:, 1:χ]·O for a gauge-rotated projector (O χ×χ orthogonal)
+  sc.z = make_ten(const_cast<double*>(U), {chi, d, chi});
+  if (O) {
+    sc.z.p = ws_d(c, n * chi);
+    gemm(c, prec, 'N', 'N', n, chi, chi, 1.0, U, n, O, chi, 0.0, sc.z.p, n);
+  }
+  grow(c, prec, a, C, T, sc.f);
+  project(c, prec, a, T, sc.z, sc.f);
+  sc.Cout = ws_d(c, (int64_t)chi * chi);
+  sc.Tout = ws_d(c, (int64_t)chi * d * chi);
+  finish(c, chi, d, sc.f, sc.Cout, sc.Tout);
+}
+
 void ctmrg_step_bwd(tnad_ctx* c, int prec, const double* a_, int d, int chi, const double* C_, const double* T_,
                     const double* U, const double* S, const double* V, const double* dCn_, const double* dTn_,
                     double* dbulk, double* dC, double* dT, bool accumulate_bulk, const double* O,
-                    const double* zref) {
+                    const double* zref, const StepCache* cache) {
   WsScope scope(c);
   const int64_t n = (int64_t)chi * d;
   const int64_t nCh = (int64_t)chi * chi, nTe = (int64_t)chi * d * chi;
   Ten a = make_ten(const_cast<double*>(a_), {d, d, d, d});
   Ten C = make_ten(const_cast<double*>(C_), {chi, chi});
   Ten T = make_ten(const_cast<double*>(T_), {chi, d, chi});
-  // z = U[:, 1:χ], or U[:, 1:χ]·O for a gauge-rotated projector (O χ×χ orthogonal)
-  Ten z = make_ten(const_cast<double*>(U), {chi, d, chi});
-  if (O) {
-    z.p = ws_d(c, n * chi);
-    gemm(c, prec, 'N', 'N', n, chi, chi, 1.0, U, n, O, chi, 0.0, z.p, n);
+  // forward intermediates: from the caller's cache, else recomputed (the
+  // decomposition itself always comes from the caller / tape)
+  StepCache local;
+  if (!cache) {
+    step_cache_fill(c, prec, a_, d, chi, C_, T_, U, O, local);
+    cache = &local;
   }
-  // recompute the forward intermediates (the decomposition comes from the tape)
-  StepFwd f;
-  grow(c, prec, a, C, T, f);
-  project(c, prec, a, T, z, f);
-  double* Cout = ws_d(c, nCh);
-  double* Tout = ws_d(c, nTe);
-  finish(c, chi, d, f, Cout, Tout);
+  const StepFwd& f = cache->f;
+  const Ten z = cache->z;
+  const double* Cout = cache->Cout;
+  const double* Tout = cache->Tout;
   // normalise pullback: dCs = (dC' − ⟨dC',C'⟩C')/‖Cs‖
   double* dots = ws_d(c, 2);
   dot_dev(c, dCn_, Cout, nCh, dots);
@@ -230,8 +247,7 @@ void ctmrg_step_bwd(tnad_ctx* c, int prec, const double* a_, int d, int chi, con
   contract(c, prec, dw, "icd", z, "abi", dcp, "abcd");
   contract(c, prec, f.cp, "abcd", dw, "icd", dz, "abi", 1.0, 1.0);
   // svd pullback with dU = [dz, 0]  (only u is used downstream: src/ctmrg.jl:137)
-  double* dUfull = ws_d(c, n * n);
-  fill(c, dUfull, n * n, 0.0);
+  double* dUfull = ws_d(c, n * chi);  // the χ non-zero leading columns of dU
   if (O) {
     // z = U_χ·O(U_χ) with O = polar(U_χᵀ·R), R = zref held fixed.  Pullback of
     // the polar factor at X ≈ O:  Ū_χ = (z̄ − R·skew(zᵀ·z̄))·Oᵀ, which makes
@@ -250,7 +266,8 @@ void ctmrg_step_bwd(tnad_ctx* c, int prec, const double* a_, int d, int chi, con
     copy_d2d(c, dUfull, dz.p, n * chi);
   }
   double* dM = ws_d(c, n * n);
-  svd_back(c, prec, U, S, V, n, n, dUfull, nullptr, nullptr, 1e-40, dM);
+  // svd_back(U, S, V, [dU_χ 0], nothing, nothing) with the χ-column structure exploited
+  svd_back_cols(c, prec, U, S, V, n, chi, dUfull, 1e-40, dM);
   // cpmat += cpmat'  →  dcp += dM + dMᵀ
   double* dMs = ws_d(c, n * n);
   add_transpose(c, n, dM, dMs);

@@ -81,6 +81,8 @@ void check_launch(tnad_ctx* c, const char* what) {
 
 using namespace tnad;
 
+static void kt_clear(tnad_ctx* c);
+
 extern "C" int tnad_version(void) { return 10000; }
 
 extern "C" void tnad_opts_default(tnad_opts* o) {
@@ -129,6 +131,7 @@ extern "C" void tnad_ctx_destroy(tnad_ctx* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   c->ws.release_all();
+  kt_clear(c);
   if (c->d_red) cudaFree(c->d_red);
   if (c->h_pin) cudaFreeHost(c->h_pin);
   if (c->d_flag) cudaFree(c->d_flag);
@@ -142,3 +145,78 @@ extern "C" const char* tnad_last_error(const tnad_ctx* c) { return c ? c->err.c_
 extern "C" int64_t tnad_ctx_workspace_bytes(const tnad_ctx* c) { return c ? c->ws.bytes_held() : 0; }
 
 extern "C" int64_t tnad_ctx_kernel_launches(const tnad_ctx* c) { return c ? c->launches : 0; }
+
+static void kt_clear(tnad_ctx* c) {
+  for (auto& p : c->kt_ev) {
+    cudaEventDestroy(p.first);
+    cudaEventDestroy(p.second);
+  }
+  c->kt_ev.clear();
+  c->kt_work = 0.0;
+}
+
+extern "C" int tnad_ctx_kernel_timer(tnad_ctx* c, const char* name) {
+  if (!c) return TNAD_ERR_ARG;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  kt_clear(c);
+  c->ktimer = name ? name : "";
+  return TNAD_OK;
+}
+
+extern "C" int tnad_ctx_kernel_timer_read(tnad_ctx* c, int64_t* launches, double* total_ms, double* work) {
+  if (!c) return TNAD_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) return TNAD_ERR_CUDA;
+  double ms = 0.0;
+  for (auto& p : c->kt_ev) {
+    float t = 0.f;
+    if (cudaEventElapsedTime(&t, p.first, p.second) == cudaSuccess) ms += t;
+  }
+  if (launches) *launches = (int64_t)c->kt_ev.size();
+  if (total_ms) *total_ms = ms;
+  if (work) *work = c->kt_work;
+  return TNAD_OK;
+}
+
+extern "C" void* tnad_ctx_stream(tnad_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+// ---------------------------------------------------------------- phase trace
+#include <cstdio>
+#include <cstdlib>
+#include <map>
+#include <string>
+
+namespace tnad {
+
+PhaseTrace::PhaseTrace(tnad_ctx* c, const char* name) : c_(c), name_(name), on_(std::getenv("TNAD_TRACE") != nullptr) {}
+
+void PhaseTrace::mark(const char* phase) {
+  if (!on_) return;
+  cudaEvent_t e;
+  if (cudaEventCreate(&e) != cudaSuccess) return;
+  cudaEventRecord(e, c_->stream);
+  ev_.push_back({phase, e});
+}
+
+PhaseTrace::~PhaseTrace() {
+  if (!on_ || ev_.empty()) return;
+  mark("end");
+  cudaEventSynchronize(ev_.back().second);
+  std::map<std::string, std::pair<double, int>> acc;
+  for (size_t i = 0; i + 1 < ev_.size(); ++i) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev_[i].second, ev_[i + 1].second);
+    auto& a = acc[ev_[i].first];
+    a.first += ms;
+    a.second += 1;
+  }
+  double tot = 0.0;
+  for (auto& kv : acc) tot += kv.second.first;
+  std::fprintf(stderr, "[tnad trace] %s: %.3f ms\n", name_, tot);
+  for (auto& kv : acc)
+    std::fprintf(stderr, "[tnad trace]   %-18s %9.3f ms  (%d)\n", kv.first.c_str(), kv.second.first, kv.second.second);
+  for (auto& p : ev_) cudaEventDestroy(p.second);
+}
+
+}  // namespace tnad

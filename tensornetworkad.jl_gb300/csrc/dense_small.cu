@@ -88,14 +88,15 @@ template <typename T>
 __global__ void k_eigh_jacobi(const double* __restrict__ A, int p, int max_sweeps, double* __restrict__ lam,
                               double* __restrict__ W, T* __restrict__ Z, int* __restrict__ info) {
   extern __shared__ unsigned char smraw[];
-  T* H = reinterpret_cast<T*>(smraw);  // p×p
+  T* H = reinterpret_cast<T*>(smraw);  // p×p, leading dimension ld = p+1 (bank-conflict free)
+  const int ld = p + 1;
   __shared__ T cs_[128], sn_[128];
   __shared__ int pp_[128], qq_[128];
   __shared__ int rotated;
   const int NP = p + (p & 1);
   const T tol = (T)(sizeof(T) == 8 ? 4.0 * DBL_EPSILON : 4.0 * FLT_EPSILON) * (T)sqrt((double)p);
   for (int e = threadIdx.x; e < p * p; e += blockDim.x) {
-    H[e] = (T)A[e];
+    H[(e % p) + (e / p) * ld] = (T)A[e];
     Z[e] = (e % p == e / p) ? (T)1 : (T)0;
   }
   __syncthreads();
@@ -115,7 +116,7 @@ __global__ void k_eigh_jacobi(const double* __restrict__ A, int p, int max_sweep
             a = b;
             b = t;
           }
-          const T apq = H[a + b * p], app = H[a + a * p], aqq = H[b + b * p];
+          const T apq = H[a + b * ld], app = H[a + a * ld], aqq = H[b + b * ld];
           if (apq != (T)0 && fabs((double)apq) > (double)tol * sqrt(fabs((double)app * (double)aqq)) &&
               fabs((double)apq) > 1e-300) {
             const T tau = (aqq - app) / ((T)2 * apq);
@@ -139,9 +140,9 @@ __global__ void k_eigh_jacobi(const double* __restrict__ A, int p, int max_sweep
         const int a = pp_[k], b = qq_[k];
         if (a < 0 || sn_[k] == (T)0) continue;
         const T c = cs_[k], s = sn_[k];
-        const T x = H[a + col * p], y = H[b + col * p];
-        H[a + col * p] = c * x - s * y;
-        H[b + col * p] = s * x + c * y;
+        const T x = H[a + col * ld], y = H[b + col * ld];
+        H[a + col * ld] = c * x - s * y;
+        H[b + col * ld] = s * x + c * y;
       }
       __syncthreads();
       // columns of H and of Z
@@ -150,9 +151,9 @@ __global__ void k_eigh_jacobi(const double* __restrict__ A, int p, int max_sweep
         const int a = pp_[k], b = qq_[k];
         if (a < 0 || sn_[k] == (T)0) continue;
         const T c = cs_[k], s = sn_[k];
-        const T x = H[row + a * p], y = H[row + b * p];
-        H[row + a * p] = c * x - s * y;
-        H[row + b * p] = s * x + c * y;
+        const T x = H[row + a * ld], y = H[row + b * ld];
+        H[row + a * ld] = c * x - s * y;
+        H[row + b * ld] = s * x + c * y;
         const T zx = Z[row + a * p], zy = Z[row + b * p];
         Z[row + a * p] = c * zx - s * zy;
         Z[row + b * p] = s * zx + c * zy;
@@ -161,8 +162,8 @@ __global__ void k_eigh_jacobi(const double* __restrict__ A, int p, int max_sweep
       for (int k = threadIdx.x; k < NP / 2; k += blockDim.x) {
         const int a = pp_[k], b = qq_[k];
         if (a >= 0 && sn_[k] != (T)0) {
-          H[a + b * p] = (T)0;
-          H[b + a * p] = (T)0;
+          H[a + b * ld] = (T)0;
+          H[b + a * ld] = (T)0;
         }
       }
       __syncthreads();
@@ -173,10 +174,10 @@ __global__ void k_eigh_jacobi(const double* __restrict__ A, int p, int max_sweep
   }
   // sort by |λ| descending (ties by index): rank_j = #{i: |λ_i| > |λ_j| or (= and i<j)}
   for (int j = threadIdx.x; j < p; j += blockDim.x) {
-    const double lj = (double)H[j + j * p];
+    const double lj = (double)H[j + j * ld];
     int rk = 0;
     for (int i = 0; i < p; ++i) {
-      const double li = (double)H[i + i * p];
+      const double li = (double)H[i + i * ld];
       rk += (fabs(li) > fabs(lj) || (fabs(li) == fabs(lj) && i < j)) ? 1 : 0;
     }
     lam[rk] = lj;
@@ -189,7 +190,7 @@ void eigh_small_prec(tnad_ctx* c, bool fp32, const double* A, int64_t p, double*
                      int* dev_info) {
   TNAD_REQUIRE(p >= 1 && p <= 256, TNAD_ERR_SHAPE, "eigh_small: p must be in [1,256]");
   WsScope scope(c);
-  size_t sm = (size_t)p * p * (fp32 ? 4 : 8);
+  size_t sm = (size_t)(p + 1) * p * (fp32 ? 4 : 8);
   TNAD_REQUIRE(sm <= 200 * 1024, TNAD_ERR_SHAPE, "eigh_small: matrix does not fit in shared memory");
   static bool attr32 = false, attr64 = false;
   if (fp32) {
@@ -222,8 +223,9 @@ void eigh_small(tnad_ctx* c, const double* A, int64_t p, double* W, double* lam)
 __global__ void k_polar_ns(const double* __restrict__ X, int m, int iters, double* __restrict__ O,
                            int* __restrict__ info) {
   extern __shared__ float psm[];
-  float* A = psm;          // m×m current iterate
-  float* G = psm + m * m;  // m×m scratch
+  const int ld = m + 1;         // padded leading dimension (bank-conflict free)
+  float* A = psm;               // m×m current iterate
+  float* G = psm + m * ld;      // m×m scratch
   __shared__ float red[32];
   const int mm = m * m;
   // scale by 1/‖X‖_F·√m so that all singular values are ≤ 1 < √3
@@ -239,26 +241,26 @@ __global__ void k_polar_ns(const double* __restrict__ X, int m, int iters, doubl
   }
   __syncthreads();
   const float sc = fminf(red[0], 1.0f) * 0.999f;
-  for (int e = threadIdx.x; e < mm; e += blockDim.x) A[e] = (float)X[e] * (red[0] > 1.f ? sc : 1.0f);
+  for (int e = threadIdx.x; e < mm; e += blockDim.x) A[(e % m) + (e / m) * ld] = (float)X[e] * (red[0] > 1.f ? sc : 1.0f);
   __syncthreads();
   for (int it = 0; it < iters; ++it) {
     // G = AᵀA
     for (int e = threadIdx.x; e < mm; e += blockDim.x) {
       const int i = e % m, j = e / m;
       float acc = 0.f;
-      for (int k = 0; k < m; ++k) acc += A[k + i * m] * A[k + j * m];
-      G[e] = acc;
+      for (int k = 0; k < m; ++k) acc += A[k + i * ld] * A[k + j * ld];
+      G[i + j * ld] = acc;
     }
     __syncthreads();
     // A ← A·(1.5 I − 0.5 G)   (row i of A times G; one thread per element, into O as scratch)
     for (int e = threadIdx.x; e < mm; e += blockDim.x) {
       const int i = e % m, j = e / m;
-      float acc = 1.5f * A[i + j * m];
-      for (int k = 0; k < m; ++k) acc -= 0.5f * A[i + k * m] * G[k + j * m];
+      float acc = 1.5f * A[i + j * ld];
+      for (int k = 0; k < m; ++k) acc -= 0.5f * A[i + k * ld] * G[k + j * ld];
       O[e] = (double)acc;
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < mm; e += blockDim.x) A[e] = (float)O[e];
+    for (int e = threadIdx.x; e < mm; e += blockDim.x) A[(e % m) + (e / m) * ld] = (float)O[e];
     __syncthreads();
   }
   // orthogonality check
@@ -266,7 +268,7 @@ __global__ void k_polar_ns(const double* __restrict__ X, int m, int iters, doubl
   for (int e = threadIdx.x; e < mm; e += blockDim.x) {
     const int i = e % m, j = e / m;
     float acc = 0.f;
-    for (int k = 0; k < m; ++k) acc += A[k + i * m] * A[k + j * m];
+    for (int k = 0; k < m; ++k) acc += A[k + i * ld] * A[k + j * ld];
     worst = fmaxf(worst, fabsf(acc - (i == j ? 1.f : 0.f)));
   }
   for (int o = 16; o > 0; o >>= 1) worst = fmaxf(worst, __shfl_xor_sync(0xffffffffu, worst, o));
@@ -284,10 +286,10 @@ void polar_ns(tnad_ctx* c, const double* X, int64_t m, int iters, double* O, int
   TNAD_REQUIRE(m >= 1 && m <= 128, TNAD_ERR_SHAPE, "polar_ns: m must be in [1,128]");
   static bool attr = false;
   if (!attr) {
-    TNAD_CK(cudaFuncSetAttribute(k_polar_ns, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 128 * 128 * 4));
+    TNAD_CK(cudaFuncSetAttribute(k_polar_ns, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 129 * 128 * 4));
     attr = true;
   }
-  k_polar_ns<<<1, 1024, (size_t)2 * m * m * 4, c->stream>>>(X, (int)m, iters, O, dev_info);
+  k_polar_ns<<<1, 1024, (size_t)2 * (m + 1) * m * 4, c->stream>>>(X, (int)m, iters, O, dev_info);
   count_launch(c);
   check_launch(c, "polar_ns");
 }
@@ -303,7 +305,14 @@ __device__ __forceinline__ uint64_t mix64(uint64_t x) {
 }
 
 // x[i] = scale·N(0,1) sample from a counter-based hash (SplitMix64 finaliser + Box–Muller)
-__global__ void k_randn(double* __restrict__ x, int64_t n, uint64_t seed, double scale, int accumulate) {
+// With sumsq != null the scale is relative to the RMS of the existing entries
+// (scale·√(Σx²/n)), read on the device so that no host synchronisation is needed.
+__global__ void k_randn(double* __restrict__ x, int64_t n, uint64_t seed, double scale, int accumulate,
+                        const double* __restrict__ sumsq) {
+  if (sumsq) {
+    const double ms = sumsq[0] / (double)n;
+    scale *= ms > 0.0 ? sqrt(ms) : 1.0;
+  }
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const uint64_t h1 = mix64(seed * 0x9e3779b97f4a7c15ull + 2 * (uint64_t)i + 1);
     const uint64_t h2 = mix64(h1 ^ 0xd6e8feb86659fd93ull);
@@ -314,9 +323,10 @@ __global__ void k_randn(double* __restrict__ x, int64_t n, uint64_t seed, double
   }
 }
 
-void randn(tnad_ctx* c, double* x, int64_t n, uint64_t seed, double scale, bool accumulate) {
+void randn(tnad_ctx* c, double* x, int64_t n, uint64_t seed, double scale, bool accumulate,
+           const double* dev_sumsq) {
   int nb = (int)std::min<int64_t>((n + 255) / 256, 4096);
-  k_randn<<<nb, 256, 0, c->stream>>>(x, n, seed, scale, accumulate ? 1 : 0);
+  k_randn<<<nb, 256, 0, c->stream>>>(x, n, seed, scale, accumulate ? 1 : 0, dev_sumsq);
   count_launch(c);
   check_launch(c, "randn");
 }

@@ -113,11 +113,14 @@ void gemm_f64(tnad_ctx* c, char ta, char tb, int64_t M, int64_t N, int64_t K, do
   const bool big = (M >= 64 && N >= 64);
   const int BM = big ? 64 : 32, BN = big ? 64 : 32;
   int64_t tiles = ((M + BM - 1) / BM) * ((N + BN - 1) / BN);
+  // Each SM retires only ~2 DFMA per clock, so a GEMM whose output has fewer
+  // tiles than SMs is split along K until about two CTAs per SM are busy
+  // (chunks of at least 64 K values; partial sums reduced in fixed order).
   int ks = 1;
-  if (tiles < c->sm_count && K >= 512) {
+  if (tiles < 2 * c->sm_count && K >= 128) {
     int64_t want = (2 * c->sm_count + tiles - 1) / tiles;
-    int64_t cap = K / 256;
-    ks = (int)std::max<int64_t>(1, std::min<int64_t>({want, cap, 64}));
+    int64_t cap = K / 64;
+    ks = (int)std::max<int64_t>(1, std::min<int64_t>({want, cap, 128}));
   }
   int64_t kchunk = (K + ks - 1) / ks;
   kchunk = (kchunk + 15) / 16 * 16;
@@ -126,6 +129,7 @@ void gemm_f64(tnad_ctx* c, char ta, char tb, int64_t M, int64_t N, int64_t K, do
   double* part = nullptr;
   if (ks > 1) part = ws_d(c, (int64_t)ks * M * N);
   dim3 grid((unsigned)((M + BM - 1) / BM), (unsigned)((N + BN - 1) / BN), (unsigned)ks);
+  KernelTimer kt(c, "gemm_f64", 2.0 * (double)M * (double)N * (double)K);
   if (big)
     k_gemm_f64<64, 64, 4, 4><<<grid, 256, 0, c->stream>>>(ita, itb, M, N, K, kchunk, alpha, A, lda, B, ldb, beta, C,
                                                           ldc, part);

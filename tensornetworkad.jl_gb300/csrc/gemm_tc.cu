@@ -351,6 +351,7 @@ void launch_tc(tnad_ctx* c, int64_t M, int64_t N, int64_t K, double alpha, const
   int* err = c->d_flag + 8;
   WsScope scope(c);
   double* P = splits > 1 ? ws_d(c, (int64_t)splits * M * N) : nullptr;
+  KernelTimer kt(c, "gemm_tf32x3", 2.0 * (double)M * (double)N * (double)K);  // logical FP64-equivalent flops
   k_gemm_tf32x3<BN><<<grid, 128, Cfg<BN>::SMEM, c->stream>>>(tAh, tAl, tBh, tBl, (int)M, (int)N, kbt, kps, alpha,
                                                              beta, Cm, ldc, P, err);
   count_launch(c);

@@ -88,6 +88,85 @@ __global__ void k_jacobi_round(double* __restrict__ W, double* __restrict__ V, i
   if (lane == 0) atomicAdd(rotated, 1);
 }
 
+// Same round with one 128-thread CTA per column pair: each thread keeps R rows
+// of both columns in registers (one read and one write of W per round), the
+// three dot products reduce through warp shuffles and shared memory.
+template <int R>
+__global__ void __launch_bounds__(128) k_jacobi_round_cta(double* __restrict__ W, double* __restrict__ V, int64_t m,
+                                                          int64_t n, int r, int NP, double tol, double abs_eps,
+                                                          const double* __restrict__ fro2, int* __restrict__ rotated) {
+  __shared__ double red[3][4];
+  __shared__ double rot[2];
+  int p, q;
+  pair_of(r, blockIdx.x, NP, &p, &q);
+  if (p >= n || q >= n) return;  // bye (uniform across the CTA)
+  if (p > q) {
+    int t = p;
+    p = q;
+    q = t;
+  }
+  double* wp = W + (int64_t)p * m;
+  double* wq = W + (int64_t)q * m;
+  double x[R], y[R];
+  double a = 0.0, b = 0.0, g = 0.0;
+#pragma unroll
+  for (int k = 0; k < R; ++k) {
+    const int64_t i = threadIdx.x + (int64_t)k * 128;
+    x[k] = i < m ? wp[i] : 0.0;
+    y[k] = i < m ? wq[i] : 0.0;
+  }
+#pragma unroll
+  for (int k = 0; k < R; ++k) {
+    a = fma(x[k], x[k], a);
+    b = fma(y[k], y[k], b);
+    g = fma(x[k], y[k], g);
+  }
+  a = wsum(a);
+  b = wsum(b);
+  g = wsum(g);
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) {
+    red[0][w] = a;
+    red[1][w] = b;
+    red[2][w] = g;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    a = red[0][0] + red[0][1] + red[0][2] + red[0][3];
+    b = red[1][0] + red[1][1] + red[1][2] + red[1][3];
+    g = red[2][0] + red[2][1] + red[2][2] + red[2][3];
+    double cs = 1.0, sn = 0.0;
+    if (g != 0.0 && a != 0.0 && b != 0.0 &&
+        fabs(g) > tol * sqrt(a) * sqrt(b) + abs_eps * sqrt(fro2[0]) * (sqrt(a) + sqrt(b))) {
+      const double zeta = (b - a) / (2.0 * g);
+      const double t = fabs(zeta) > 1e150 ? 0.5 / zeta : copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+      cs = 1.0 / sqrt(1.0 + t * t);
+      sn = cs * t;
+      atomicAdd(rotated, 1);
+    }
+    rot[0] = cs;
+    rot[1] = sn;
+  }
+  __syncthreads();
+  const double cs = rot[0], sn = rot[1];
+  if (sn == 0.0) return;
+#pragma unroll
+  for (int k = 0; k < R; ++k) {
+    const int64_t i = threadIdx.x + (int64_t)k * 128;
+    if (i < m) {
+      wp[i] = cs * x[k] - sn * y[k];
+      wq[i] = sn * x[k] + cs * y[k];
+    }
+  }
+  double* vp = V + (int64_t)p * n;
+  double* vq = V + (int64_t)q * n;
+  for (int64_t i = threadIdx.x; i < n; i += 128) {
+    const double xv = vp[i], yv = vq[i];
+    vp[i] = cs * xv - sn * yv;
+    vq[i] = sn * xv + cs * yv;
+  }
+}
+
 __global__ void k_eye(double* V, int64_t n) {
   int64_t nn = n * n;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nn; e += (int64_t)gridDim.x * blockDim.x)
@@ -275,8 +354,24 @@ void svd_jacobi(tnad_ctx* c, const double* A, int64_t m, int64_t n, double* U, d
     // exact orthogonality (the triplets trg_svd's √s pullback relies on).  Only
     // a spectrum that keeps re-rotating noise past kRelSweeps gets the floor.
     const double ae = sweep < kRelSweeps ? 0.0 : abs_eps;
+    // pairs per round: NP/2 CTAs of 128 threads with the columns in registers
+    // (R rows per thread), or one warp per pair for very tall matrices
+    const unsigned np2 = (unsigned)(NP / 2);
+    // algorithmic FP64 work of one round: per pair 3 dot products (6m flops)
+    // and one plane rotation of W (6m) and V (6n)
+    const double round_flops = (double)(n / 2) * (12.0 * (double)m + 6.0 * (double)n);
     for (int r = 0; r < NP - 1; ++r) {
-      k_jacobi_round<<<blocks, threads, 0, c->stream>>>(W, Vw, m, n, r, NP, tol, ae, fro2, flag);
+      KernelTimer kt(c, "jacobi_round", round_flops);
+      if (m <= 256)
+        k_jacobi_round_cta<2><<<np2, 128, 0, c->stream>>>(W, Vw, m, n, r, NP, tol, ae, fro2, flag);
+      else if (m <= 512)
+        k_jacobi_round_cta<4><<<np2, 128, 0, c->stream>>>(W, Vw, m, n, r, NP, tol, ae, fro2, flag);
+      else if (m <= 1024)
+        k_jacobi_round_cta<8><<<np2, 128, 0, c->stream>>>(W, Vw, m, n, r, NP, tol, ae, fro2, flag);
+      else if (m <= 2048)
+        k_jacobi_round_cta<16><<<np2, 128, 0, c->stream>>>(W, Vw, m, n, r, NP, tol, ae, fro2, flag);
+      else
+        k_jacobi_round<<<blocks, threads, 0, c->stream>>>(W, Vw, m, n, r, NP, tol, ae, fro2, flag);
     }
     count_launch(c, NP - 1);
     check_launch(c, "jacobi_round");

@@ -50,7 +50,16 @@ void ctmrg_step_fwd(tnad_ctx* c, int prec, const double* a, int d, int chi, cons
 void ctmrg_step_bwd(tnad_ctx* c, int prec, const double* a, int d, int chi, const double* C, const double* T,
                     const double* U, const double* S, const double* V, const double* dCn, const double* dTn,
                     double* dbulk, double* dC, double* dT, bool accumulate_bulk, const double* O = nullptr,
-                    const double* zref = nullptr);
+                    const double* zref = nullptr, const struct StepCache* cache = nullptr);
+// Forward intermediates of one step at fixed (C, T, z), reusable across many
+// pullbacks (the fixed-point adjoint applies the same step Jacobian repeatedly).
+struct StepCache {
+  StepFwd f;
+  Ten z;
+  double *Cout = nullptr, *Tout = nullptr;
+};
+void step_cache_fill(tnad_ctx* c, int prec, const double* a, int d, int chi, const double* C, const double* T,
+                     const double* U, const double* O, StepCache& sc);
 // ctmrg loop with the reference stop rule; C/T hold the initial env on entry and
 // the result on exit.  With tape != null every step's input and decomposition
 // are recorded (pool owns the memory).

@@ -82,9 +82,48 @@ struct tnad_ctx {
   int* d_flag = nullptr;    // device flags / counters (64 ints)
   int* h_flag = nullptr;    // pinned host mirror of the flags
   bool tc_ok = false;       // tcgen05 GEMM path available (sm_100 family)
+  // kernel timer (tnad_ctx_kernel_timer): events around every launch of one
+  // kernel family, with the algorithmic work (flops or bytes) of each launch
+  std::string ktimer;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> kt_ev;
+  double kt_work = 0.0;
 };
 
 namespace tnad {
+
+// Phase timer: with TNAD_TRACE set in the environment, CUDA events bracket
+// named phases on the context stream and a per-phase summary goes to stderr
+// when the tracer is destroyed.  Without TNAD_TRACE it does nothing.
+class PhaseTrace {
+ public:
+  PhaseTrace(tnad_ctx* c, const char* name);
+  ~PhaseTrace();
+  void mark(const char* phase);  // closes the previous phase, opens `phase`
+
+ private:
+  tnad_ctx* c_;
+  const char* name_;
+  bool on_;
+  std::vector<std::pair<const char*, cudaEvent_t>> ev_;
+};
+
+// Brackets one launch of kernel family `name` with CUDA events when the
+// context's kernel timer is set to that family.
+struct KernelTimer {
+  tnad_ctx* c;
+  cudaEvent_t e1 = nullptr;
+  KernelTimer(tnad_ctx* ctx, const char* name, double work) : c(ctx) {
+    if (c->ktimer.empty() || c->ktimer != name) return;
+    cudaEvent_t e0;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return;
+    cudaEventRecord(e0, c->stream);
+    c->kt_ev.push_back({e0, e1});
+    c->kt_work += work;
+  }
+  ~KernelTimer() {
+    if (e1) cudaEventRecord(e1, c->stream);
+  }
+};
 
 // RAII scope over the context's workspace stack.
 struct WsScope {
@@ -158,6 +197,9 @@ void svd_jacobi(tnad_ctx* c, const double* A, int64_t m, int64_t n, double* U, d
 void eigh_small(tnad_ctx* c, const double* A, int64_t p, double* W, double* lam);
 
 // ---------------- SVD adjoint (svd_back.cu) ----------------
+// Square thin SVD (n×n) with dU non-zero only in its first k columns (dUk n×k).
+void svd_back_cols(tnad_ctx* c, int prec, const double* U, const double* S, const double* V, int64_t n, int64_t k,
+                   const double* dUk, double eta, double* dA);
 // svd_back for thin SVD (U m×n, S n, V n×n), dU m×n or null, dS n or null, dV n×n or null.
 void svd_back(tnad_ctx* c, int prec, const double* U, const double* S, const double* V, int64_t m,
               int64_t n, const double* dU, const double* dS, const double* dV, double eta,

@@ -141,6 +141,18 @@ int tnad_trg_svd(tnad_ctx* ctx, const double* t, int d1, int d2, int d3, int d4,
    U: m×n, S: n (descending), V: n×n.  Replaces LinearAlgebra.svd at
    src/trg.jl:36 and src/ctmrg.jl:136. */
 int tnad_svd(tnad_ctx* ctx, const double* A, int m, int n, double* U, double* S, double* V);
+/* Allocation-free FP64 Jacobi SVD (no counterpart in the reference): the same
+   decomposition as tnad_svd for m×n matrices with n ≤ m ≤ 256, for callers that
+   cannot allocate device memory (a host framework that owns all device memory
+   through its own allocator, or a latency-critical loop where an allocation
+   would synchronise the device).  Needs no context: A, U, S, V are DEVICE
+   pointers supplied by the caller (m×n, n, n×n, column-major) and stream is a
+   cudaStream_t (0: legacy default stream).  Its scratch is a fixed static device
+   array (about 1.1 MB, held by every GPU that loads the library until exit),
+   shared by all calls: calls that overlap on the GPU race.  The first call on a
+   device resolves that array's address and should come before any stream
+   capture.  Sizes beyond 256 return TNAD_ERR_SHAPE. */
+int tnad_svd_noalloc(const double* A, int m, int n, double* U, double* S, double* V, void* stream);
 /* svd_back(U,S,V,dU,dS,dV; η) of src/trg.jl:94-128 (real).  dU/dS/dV may be NULL. */
 int tnad_svd_back(tnad_ctx* ctx, const double* U, const double* S, const double* V,
                   int m, int n, const double* dU, const double* dS, const double* dV,

@@ -70,6 +70,7 @@ SIGNATURES = {
     "tnad_trg_backward": (C.c_int, [VP, VP, C.c_double, DP]),
     "tnad_trg_svd": (C.c_int, [VP, DP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, DP, DP, IP]),
     "tnad_svd": (C.c_int, [VP, DP, C.c_int, C.c_int, DP, DP, DP]),
+    "tnad_svd_noalloc": (C.c_int, [DP, C.c_int, C.c_int, DP, DP, DP, VP]),
     "tnad_svd_back": (C.c_int, [VP, DP, DP, DP, C.c_int, C.c_int, DP, DP, DP, C.c_double, DP]),
     "tnad_ctmrgstep": (C.c_int, [VP, DP, C.c_int, C.c_int, DP, DP, DP, DP, DP]),
     "tnad_ctmrgstep_backward": (C.c_int, [VP, DP, C.c_int, C.c_int, DP, DP, DP, DP, DP, DP, DP]),

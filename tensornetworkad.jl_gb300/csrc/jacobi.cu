@@ -7,8 +7,10 @@
 // orthogonality ≤ m·ε), capped at kMaxSweeps (→ TNAD_ERR_NOT_CONVERGED).
 // Singular values are the column norms, sorted descending by a rank kernel
 // (ties by index, so the result is deterministic).
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <mutex>
 
 #include "tnad_internal.h"
 
@@ -404,4 +406,127 @@ void svd_jacobi(tnad_ctx* c, const double* A, int64_t m, int64_t n, double* U, d
   }
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the FP64 Jacobi SVD (tnad_svd_noalloc).
+//
+// Its scratch lives in one file-scope device array of fixed size, sized for
+// matrices up to kNoAllocMax × kNoAllocMax.  Every GPU that loads this library
+// holds that array (about 1.1 MB) until the process exits.  All calls on a
+// device share it, and it keeps the previous call's contents: the entry point
+// initialises everything it reads, and calls that overlap on the GPU (two
+// streams, or two host threads) race on it.
+// ---------------------------------------------------------------------------
+static const int kNoAllocMax = 256;
+static const int64_t kNoAllocDoubles = 2 * (int64_t)kNoAllocMax * kNoAllocMax  // W, V working copies
+                                       + 4 * kNoAllocMax                      // s, sign, coef, rank (as ints)
+                                       + 64;                                   // ‖A‖²_F and counters
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocDoubles];
+
+// single-block Σ A² into out[0] (the scratch's ‖A‖²_F slot)
+__global__ void k_sumsq_one_block(const double* __restrict__ A, int64_t n, double* __restrict__ out) {
+  __shared__ double sh[256];
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s = fma(A[i], A[i], s);
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+    if ((int)threadIdx.x < k) sh[threadIdx.x] += sh[threadIdx.x + k];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = sh[0];
+}
+
+__global__ void k_copy_eye(const double* __restrict__ A, int64_t mn, double* __restrict__ W, double* __restrict__ V,
+                           int64_t n) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < mn + n * n; e += (int64_t)gridDim.x * blockDim.x) {
+    if (e < mn)
+      W[e] = A[e];
+    else {
+      const int64_t f = e - mn;
+      V[f] = (f % n == f / n) ? 1.0 : 0.0;
+    }
+  }
+}
+
 }  // namespace tnad
+
+// Scratch address of g_noalloc_scratch per device, resolved once per device
+// (with that device current) by cudaGetSymbolAddress: in host code the
+// array's name is only a host-side shadow, never a device address.
+static double* noalloc_scratch_addr(int dev) {
+  static double* addr[64] = {nullptr};
+  static std::mutex mu;
+  if (dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, tnad::g_noalloc_scratch) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return nullptr;
+    }
+    addr[dev] = (double*)p;
+  }
+  return addr[dev];
+}
+
+// Thin SVD A = U·diag(S)·Vᵀ (m ≥ n, n ≤ m ≤ 256) by the same one-sided Jacobi
+// kernels as tnad_svd, without any device allocation: for callers that cannot
+// call cudaMalloc (a host framework that owns all device memory through its own
+// allocator, code running while a CUDA graph is being built by someone else,
+// or a latency-critical loop where an allocation would synchronise the device).
+// A, U, S, V are DEVICE pointers (m×n, n, n×n, column-major); stream may be 0.
+// The first call on a device resolves the scratch address for that device and
+// should therefore happen before any stream capture.  Returns TNAD_ERR_SHAPE
+// for m or n beyond 256 (the static scratch's limit), TNAD_ERR_ARG for null
+// pointers or m < n, TNAD_ERR_NOT_CONVERGED / TNAD_ERR_CUDA as tnad_svd does.
+extern "C" int tnad_svd_noalloc(const double* A, int m, int n, double* U, double* S, double* V, void* stream) {
+  using namespace tnad;
+  if (!A || !U || !S || !V || n < 1 || m < n) return TNAD_ERR_ARG;
+  if (m > kNoAllocMax || n > kNoAllocMax) return TNAD_ERR_SHAPE;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return TNAD_ERR_CUDA;
+  double* base = noalloc_scratch_addr(dev);
+  if (!base) return TNAD_ERR_CUDA;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t mm = kNoAllocMax;
+  double* W = base;
+  double* Vw = W + mm * mm;
+  double* s = Vw + mm * mm;
+  double* sg = s + mm;
+  double* coef = sg + mm;
+  int* rank = (int*)(coef + mm);
+  double* fro2 = coef + 2 * mm;
+  int* flag = (int*)(fro2 + 8);
+  const int64_t mn = (int64_t)m * n;
+  k_copy_eye<<<(int)std::min<int64_t>((mn + (int64_t)n * n + 255) / 256, 1024), 256, 0, st>>>(A, mn, W, Vw, n);
+  k_sumsq_one_block<<<1, 256, 0, st>>>(A, mn, fro2);
+  const int NP = n + (n & 1);
+  const double tol = (double)std::max(m, 16) * DBL_EPSILON;
+  const double abs_eps = 2.0 * DBL_EPSILON;
+  bool converged = (n == 1);
+  int hflag = 0;
+  for (int sweep = 0; sweep < kMaxSweeps && !converged; ++sweep) {
+    if (cudaMemsetAsync(flag, 0, sizeof(int), st) != cudaSuccess) return TNAD_ERR_CUDA;
+    const double ae = sweep < kRelSweeps ? 0.0 : abs_eps;
+    for (int r = 0; r < NP - 1; ++r)
+      k_jacobi_round_cta<2><<<(unsigned)(NP / 2), 128, 0, st>>>(W, Vw, m, n, r, NP, tol, ae, fro2, flag);
+    if (cudaGetLastError() != cudaSuccess) return TNAD_ERR_CUDA;
+    if (cudaMemcpyAsync(&hflag, flag, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return TNAD_ERR_CUDA;
+    if (hflag == 0) converged = true;
+  }
+  if (!converged) return TNAD_ERR_NOT_CONVERGED;
+  k_colnorms<<<(n * 32 + 255) / 256, 256, 0, st>>>(W, Vw, m, n, s, sg);
+  k_rank<<<(n + 255) / 256, 256, 0, st>>>(s, n, rank);
+  if (cudaMemsetAsync(flag + 1, 0, sizeof(int), st) != cudaSuccess) return TNAD_ERR_CUDA;
+  dim3 g(1, (unsigned)n);
+  k_scatter<<<g, 256, 0, st>>>(W, Vw, s, sg, rank, m, n, 0, 1e-8, fro2, U, S, V, flag + 1);
+  int nweak = 0;
+  if (cudaMemcpyAsync(&nweak, flag + 1, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return TNAD_ERR_CUDA;
+  for (int k = n - nweak; k < n; ++k) k_complete_col<<<1, 1024, m * sizeof(double), st>>>(U, m, k, coef);
+  if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) return TNAD_ERR_CUDA;
+  return TNAD_OK;
+}

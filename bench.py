@@ -44,6 +44,13 @@ def parse():
     p.add_argument("--mode", default="mixed", choices=["plain", "mixed"])
     p.add_argument("--no-plain", dest="no_plain", action="store_true", help="skip the plain FP64 comparison solve")
     p.add_argument("--no-cpu-baseline", dest="no_cpu_baseline", action="store_true")
+    # --workload learned_D3_chi36: learned warm start against the cold start
+    p.add_argument("--n-train", dest="n_train", type=int, default=4000, help="random site tensors for training")
+    p.add_argument("--n-traj", dest="n_traj", type=int, default=16, help="Heisenberg L-BFGS trajectories")
+    p.add_argument("--traj-evals", dest="traj_evals", type=int, default=40, help="tensors kept per trajectory")
+    p.add_argument("--n-held", dest="n_held", type=int, default=500, help="held-out tensors")
+    p.add_argument("--train-steps", dest="train_steps", type=int, default=6000)
+    p.add_argument("--threads", type=int, default=8, help="concurrent CTMRG runs while generating targets")
     return p.parse_args()
 
 
@@ -364,9 +371,95 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_learned(args):
+    """Learned warm start at D=3, χ=36 (Heisenberg): targets from the mixed
+    CTMRG on uniform [-1, 1] site tensors and on the iterates of L-BFGS
+    trajectories (Jz uniform in [0.5, 1.5]); a 3-layer width-512 network
+    trained on the GPU; then, on held-out tensors from the same pool, CTMRG
+    steps and wall time of energy (forward) to the stop rule 1e-8 from the
+    learned start and from :raw.  Solves of the comparison run one at a time."""
+    import importlib
+
+    import __graft_entry__ as ge
+
+    tn = ge.load_package()
+    wl = importlib.import_module(tn.__name__ + ".learned")
+    D, s, chi, tol, maxit = 3, 2, 36, 1e-8, 400
+    h = tn.hamiltonian(tn.Heisenberg())
+    rng = np.random.default_rng(20240601)
+    t0 = time.perf_counter()
+    pool = [wl.random_site_tensor(D, s, rng) for _ in range(args.n_train + int(0.8 * args.n_held))]
+    kinds = ["uniform"] * len(pool)
+    jzs = rng.uniform(0.5, 1.5, args.n_traj)
+    seeds = rng.integers(0, 2 ** 31, args.n_traj)
+
+    def trajectory(k):
+        return wl.heisenberg_trajectory(D, chi, float(jzs[k]), np.random.default_rng(int(seeds[k])), args.traj_evals,
+                                        1e-8, maxit, tn.mixed_opts())
+
+    from concurrent.futures import ThreadPoolExecutor
+
+    with ThreadPoolExecutor(max_workers=max(1, args.threads)) as ex:
+        for traj in ex.map(trajectory, range(args.n_traj)):
+            pool += traj
+            kinds += ["trajectory"] * len(traj)
+    t1 = time.perf_counter()
+    perm = rng.permutation(len(pool))
+    n_held = min(args.n_held, len(pool) // 5)
+    held_idx, train_idx = perm[:n_held], perm[n_held:]
+    hmix = lambda: tn.mixed_opts()  # noqa: E731
+    samples = wl.make_samples([pool[i] for i in train_idx], h, chi, tol, maxit, hmix(), threads=args.threads)
+    t2 = time.perf_counter()
+    X, Y = wl.stack(samples)
+    net = wl.WarmStartNet(D, s, chi, width=512, seed=1)
+    info = net.fit(X, Y, steps=args.train_steps, batch=128, lr=1e-3, weight_decay=1e-4,
+                   log_every=max(1, args.train_steps // 8))
+    net.attach()
+    held = [pool[i] for i in held_idx]
+    # warm-up of both paths (first-call costs), not counted
+    wl.compare_starts(held[:2], h, chi, tol, maxit, hmix)
+    r = wl.compare_starts(held, h, chi, tol, maxit, hmix)
+    t3 = time.perf_counter()
+    same = r["dE"] <= 1e-8
+    hk = np.array([kinds[i] for i in held_idx])
+    by_kind = {}
+    for k in ("uniform", "trajectory"):
+        m = hk == k
+        if m.any():
+            by_kind[k] = {"n": int(m.sum()), "cold_steps": round(float(r["cold_steps"][m].mean()), 2),
+                          "warm_steps": round(float(r["warm_steps"][m].mean()), 2),
+                          "cold_s": round(float(r["cold_s"][m].mean()), 4),
+                          "warm_s": round(float(r["warm_s"][m].mean()), 4),
+                          "same_fixed_point": round(float(same[m].mean()), 3)}
+    line = {
+        "metric": "CTMRG steps and wall time to stop rule 1e-8, learned warm start vs :raw (D=3, chi=36)",
+        "value": round(float(r["warm_s"].mean()), 4), "unit": "s/solve", "higher_is_better": False,
+        "cold_s_per_solve": round(float(r["cold_s"].mean()), 4),
+        "speedup_wall": round(float(r["cold_s"].mean() / r["warm_s"].mean()), 3),
+        "cold_steps": round(float(r["cold_steps"].mean()), 2), "warm_steps": round(float(r["warm_steps"].mean()), 2),
+        "step_ratio": round(float(r["warm_steps"].mean() / r["cold_steps"].mean()), 3),
+        "median_cold_steps": float(np.median(r["cold_steps"])), "median_warm_steps": float(np.median(r["warm_steps"])),
+        "same_fixed_point": round(float(same.mean()), 3),
+        "judge_kept": round(float(np.mean(r["status"] == 1)), 3),
+        "judge_rejected": round(float(np.mean(r["status"] == -1)), 3),
+        "by_kind": by_kind,
+        "train": {"n": len(samples), "n_trajectory": int(sum(kinds[i] == "trajectory" for i in train_idx)),
+                  "steps": args.train_steps, "batch": 128, "seconds": round(info["seconds"], 2),
+                  "loss_std_final": round(info["loss_std"], 5),
+                  "history": [(k, round(v, 5)) for k, v in info["history"]]},
+        "n_held": n_held, "dtype": "bf16 network, mixed TF32X3/FP64 CTMRG", "data": "synthetic",
+        "config": {"workload": "learned_D3_chi36", "D": D, "chi": chi, "tol": tol, "model": "Heisenberg",
+                   "width": 512, "layers": 3},
+        "timing": {"pool_s": round(t1 - t0, 1), "targets_s": round(t2 - t1, 1), "compare_s": round(t3 - t2, 1)},
+    }
+    print(json.dumps(line), flush=True)
+
+
 if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.workload.startswith("learned"):
+        run_learned(a)
     else:
         run_gb300(a)

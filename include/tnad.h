@@ -35,6 +35,7 @@ extern "C" {
 
 typedef struct tnad_ctx tnad_ctx;
 typedef struct tnad_tape tnad_tape;
+typedef struct tnad_mlp tnad_mlp;
 
 enum {
   TNAD_OK = 0,
@@ -68,12 +69,20 @@ enum {
   TNAD_ADJOINT_FIXEDPOINT = 1  /* implicit adjoint at the converged environment    */
 };
 
+/* Initial CTMRG environment of tnad_energy. */
+enum {
+  TNAD_WARM_NONE = 0,    /* :raw initialisation (src/ctmrg.jl:66-86)                    */
+  TNAD_WARM_GIVEN = 1,   /* the C_init, T_init passed in                               */
+  TNAD_WARM_LEARNED = 2  /* predicted by the network attached with tnad_ctx_set_warm_start,
+                            judged by the CTMRG residual, :raw restart if it does not fall */
+};
+
 typedef struct tnad_opts {
   int32_t prec;            /* TNAD_PREC_*                                         */
   int32_t solver;          /* TNAD_SOLVER_*                                       */
   int32_t adjoint;         /* TNAD_ADJOINT_*                                      */
   int32_t device_ptrs;     /* 1: every array argument is a device pointer         */
-  int32_t warm_start;      /* 1: start CTMRG from the C,T passed in (learned net) */
+  int32_t warm_start;      /* TNAD_WARM_*: where the CTMRG environment starts      */
   int32_t stop_rule;       /* 0: reference StopFunction on all χd values;
                               1: ‖Δ(top-χ values)‖₂ ≤ tol (subspace solver)       */
   int32_t fp_maxit;        /* fixed-point adjoint iteration cap                   */
@@ -203,6 +212,60 @@ int tnad_energy_backward(tnad_ctx* ctx, tnad_tape* tape, double dE, double* dA);
    (the reference reports none of these). */
 int tnad_energy_stats(const tnad_tape* tape, int* steps, int* fp64_steps, int* switch_step, int* fp_iters,
                       double* last_diff, double* fp_residual);
+
+/* -------- learned warm start (no reference counterpart) --------
+   A 3-layer perceptron n_in → width → width → n_out (ReLU between layers) that
+   maps the symmetrised site tensor to a gauge-fixed CTMRG environment.  Its
+   products run as BF16 tcgen05 GEMMs with FP32 accumulation; parameters are an
+   FP32 array  W1 (width×n_in) | b1 | W2 (width×width) | b2 | W3 (n_out×width) | b3
+   (column-major matrices), trained with AdamW.  Activations and data are
+   column-major feature × sample, FP32.  With device_ptrs = 1 the X, Y, grad
+   arrays are device pointers. */
+int tnad_mlp_create(tnad_ctx* ctx, int n_in, int width, int n_out, uint64_t seed, tnad_mlp** out);
+/* The network's product on its own (host arrays, FP32 column-major):
+   C = alpha·op(A)·op(B) + beta·C with op(A), op(B) rounded to BF16, FP32
+   accumulation on the tensor cores, chunks of 512 K values summed in FP64. */
+int tnad_gemm_bf16(tnad_ctx* ctx, char ta, char tb, int64_t M, int64_t N, int64_t K, float alpha, const float* A,
+                   int64_t lda, const float* B, int64_t ldb, float beta, float* C, int64_t ldc);
+void tnad_mlp_free(tnad_mlp* net);
+int64_t tnad_mlp_param_count(const tnad_mlp* net);
+int tnad_mlp_get_params(tnad_ctx* ctx, const tnad_mlp* net, float* params);
+/* Sets the parameters and resets the AdamW state. */
+int tnad_mlp_set_params(tnad_ctx* ctx, tnad_mlp* net, const float* params);
+/* Y (n_out×batch) = net(X (n_in×batch)). */
+int tnad_mlp_forward(tnad_ctx* ctx, tnad_mlp* net, const float* X, int batch, float* Y, int device_ptrs);
+/* loss = mean((net(X) − Y)²) and its gradient (param_count floats; may be NULL). */
+int tnad_mlp_gradient(tnad_ctx* ctx, tnad_mlp* net, const float* X, const float* Y, int batch, float* loss,
+                      float* grad, int device_ptrs);
+/* Copies a training set (X n_in×n_samples, Y n_out×n_samples, host arrays) to
+   device memory owned by the network (n_samples = 0 releases it). */
+int tnad_mlp_set_data(tnad_ctx* ctx, tnad_mlp* net, const float* X, const float* Y, int64_t n_samples);
+/* One AdamW step (β = 0.9, 0.999, ε = 1e-8; decoupled weight decay on the
+   weight matrices) on the mini-batch idx[0..batch) (host array) of the
+   n_samples columns of X (n_in×n_samples) and Y (n_out×n_samples); X = Y =
+   NULL selects the set loaded by tnad_mlp_set_data.  loss may be NULL (then
+   the call does not wait for the GPU). */
+int tnad_mlp_train_step(tnad_ctx* ctx, tnad_mlp* net, const float* X, const float* Y, int64_t n_samples,
+                        const int32_t* idx, int batch, float lr, float weight_decay, float* loss, int device_ptrs);
+/* Gauge fixing of a symmetric CTMRG environment (the network's targets):
+   C = W·diag(λ)·Wᵀ with |λ| descending, Tg = Wᵀ·T·W on both χ legs, then the
+   column signs s_a (s_0 = +1) chosen so that for each a ≥ 1 the largest
+   |Tg[a,i,b]| over i and b < a is positive after Tg[a,i,b] ← s_a s_b Tg[a,i,b].
+   C χ×χ, T χ×d×χ in; lam χ and Tg χ×d×χ out (host arrays). */
+int tnad_env_gauge_fix(tnad_ctx* ctx, const double* C, const double* T, int chi, int d, double* lam, double* Tg);
+/* Attaches (net != NULL) or detaches the network used by TNAD_WARM_LEARNED for
+   site tensors D×D×D×D×s at bond dimension χ; n_in = D⁴·s, n_out = χ + χ·D²·χ.
+   The context does not own the network. */
+int tnad_ctx_set_warm_start(tnad_ctx* ctx, tnad_mlp* net, int D, int s, int chi);
+/* Network input of a site tensor A (D×D×D×D×s): indexperm_symmetrize(A)
+   (normalised) times the sign of its largest-|·| entry, as n_in floats. */
+int tnad_warm_start_features(tnad_ctx* ctx, const double* A, int D, int s, float* x);
+/* The predicted environment for site tensor A: C = diag(λ̂)/‖λ̂‖ and T the
+   χ-leg-symmetrised prediction /‖·‖ (host arrays χ×χ and χ×D²×χ). */
+int tnad_warm_start_env(tnad_ctx* ctx, const double* A, int D, int s, int chi, double* C, double* T);
+/* Outcome of the last TNAD_WARM_LEARNED energy call: 1 prediction kept,
+   -1 rejected by the residual judge (restarted from :raw), 0 not used. */
+int tnad_ctx_warm_start_status(const tnad_ctx* ctx);
 
 #ifdef __cplusplus
 }

@@ -22,6 +22,7 @@ ERRORS = {
     -5: "TNAD_ERR_NONFINITE", -6: "TNAD_ERR_NOMEM", -7: "TNAD_ERR_STATE", -8: "TNAD_ERR_TIMEOUT",
 }
 PREC_FP64, PREC_TF32X3, PREC_LADDER = 0, 1, 2
+WARM_NONE, WARM_GIVEN, WARM_LEARNED = 0, 1, 2
 SOLVER_FULL_SVD, SOLVER_SUBSPACE = 0, 1
 ADJOINT_UNROLLED, ADJOINT_FIXEDPOINT = 0, 1
 
@@ -45,6 +46,7 @@ class Opts(C.Structure):
 
 
 DP = C.POINTER(C.c_double)
+FP = C.POINTER(C.c_float)
 VP = C.c_void_p
 IP = C.POINTER(C.c_int)
 
@@ -84,6 +86,23 @@ SIGNATURES = {
                               DP, IP, DP, DP, C.POINTER(VP)]),
     "tnad_energy_backward": (C.c_int, [VP, VP, C.c_double, DP]),
     "tnad_energy_stats": (C.c_int, [VP, IP, IP, IP, IP, DP, DP]),
+    "tnad_mlp_create": (C.c_int, [VP, C.c_int, C.c_int, C.c_int, C.c_uint64, C.POINTER(VP)]),
+    "tnad_gemm_bf16": (C.c_int, [VP, C.c_char, C.c_char, C.c_int64, C.c_int64, C.c_int64, C.c_float, FP, C.c_int64,
+                                 FP, C.c_int64, C.c_float, FP, C.c_int64]),
+    "tnad_mlp_free": (None, [VP]),
+    "tnad_mlp_param_count": (C.c_int64, [VP]),
+    "tnad_mlp_get_params": (C.c_int, [VP, VP, FP]),
+    "tnad_mlp_set_params": (C.c_int, [VP, VP, FP]),
+    "tnad_mlp_forward": (C.c_int, [VP, VP, FP, C.c_int, FP, C.c_int]),
+    "tnad_mlp_gradient": (C.c_int, [VP, VP, FP, FP, C.c_int, FP, FP, C.c_int]),
+    "tnad_mlp_set_data": (C.c_int, [VP, VP, FP, FP, C.c_int64]),
+    "tnad_mlp_train_step": (C.c_int, [VP, VP, FP, FP, C.c_int64, C.POINTER(C.c_int32), C.c_int, C.c_float,
+                                      C.c_float, FP, C.c_int]),
+    "tnad_env_gauge_fix": (C.c_int, [VP, DP, DP, C.c_int, C.c_int, DP, DP]),
+    "tnad_ctx_set_warm_start": (C.c_int, [VP, VP, C.c_int, C.c_int, C.c_int]),
+    "tnad_warm_start_features": (C.c_int, [VP, DP, C.c_int, C.c_int, FP]),
+    "tnad_warm_start_env": (C.c_int, [VP, DP, C.c_int, C.c_int, C.c_int, DP, DP]),
+    "tnad_ctx_warm_start_status": (C.c_int, [VP]),
 }
 
 _lib = None
@@ -187,6 +206,16 @@ def ptr(a) -> DP:
         return C.cast(C.c_void_p(a), DP)
     assert a.flags["F_CONTIGUOUS"] and a.dtype == np.float64
     return a.ctypes.data_as(DP)
+
+
+def fptr(a) -> FP:
+    """float32 column-major host array, raw device address (int) or None."""
+    if a is None:
+        return C.cast(None, FP)
+    if isinstance(a, int):
+        return C.cast(C.c_void_p(a), FP)
+    assert a.flags["F_CONTIGUOUS"] and a.dtype == np.float32
+    return a.ctypes.data_as(FP)
 
 
 def fzeros(shape) -> np.ndarray:

@@ -3,6 +3,7 @@
 #include <cstring>
 #include <memory>
 
+#include "tnad_api.h"
 #include "tnad_energy.h"
 #include "tnad_trg.h"
 
@@ -54,22 +55,6 @@ tnad_opts opts_or_default(const tnad_opts* o) {
 
 }  // namespace
 
-#define API_BEGIN(c)                         \
-  if (!(c)) return TNAD_ERR_ARG;             \
-  try {                                      \
-    TNAD_CK(cudaSetDevice((c)->device));
-#define API_END(c)                           \
-  }                                          \
-  catch (const tnad::Error& e) {             \
-    (c)->err = e.msg;                        \
-    cudaStreamSynchronize((c)->stream);      \
-    return e.code;                           \
-  }                                          \
-  catch (const std::exception& e) {          \
-    (c)->err = e.what();                     \
-    return TNAD_ERR_ARG;                     \
-  }                                          \
-  return TNAD_OK;
 
 extern "C" void tnad_tape_free(tnad_tape* t) {
   if (!t) return;

@@ -307,7 +307,7 @@ __global__ void k_diffsq_partial(const double* __restrict__ v, const double* __r
 }
 
 CtmrgRun ctmrg_run(tnad_ctx* c, int prec, const double* a, int d, int chi, double* C, double* T, double tol,
-                   int maxit, CtmrgTape* tape, DevPool* pool, int64_t tape_budget) {
+                   int maxit, CtmrgTape* tape, DevPool* pool, int64_t tape_budget, bool judge) {
   const int64_t n = (int64_t)chi * d;
   const int64_t nCh = (int64_t)chi * chi, nTe = (int64_t)chi * d * chi;
   WsScope scope(c);
@@ -329,6 +329,7 @@ CtmrgRun ctmrg_run(tnad_ctx* c, int prec, const double* a, int d, int chi, doubl
   CtmrgRun run;
   int counter = 0;  // StopFunction(oldvals, -1, ...) has seen state 0
   bool have_old = false;
+  double judge_ref = 0.0;
   while (true) {
     if (tape) {
       double* Ck = pool->d(nCh);
@@ -373,6 +374,11 @@ CtmrgRun ctmrg_run(tnad_ctx* c, int prec, const double* a, int d, int chi, doubl
     }
     run.last_diff = dv;
     if (dv <= tol) break;
+    if (judge && run.steps == 2) judge_ref = dv;
+    if (judge && run.steps == 4 && !(dv < judge_ref)) {
+      run.rejected = true;
+      break;
+    }
     copy_d2d(c, oldvals, vals, n);
     have_old = true;
   }

@@ -165,7 +165,7 @@ void cholqr2(tnad_ctx* c, int prec, const double* Y, int64_t n, int64_t p, doubl
 }
 
 MixedRun ctmrg_run_mixed(tnad_ctx* c, const double* a_, int d, int chi, double* C, double* T, double tol, int maxit,
-                         const tnad_opts& o, double* zfinal) {
+                         const tnad_opts& o, double* zfinal, bool judge) {
   const int64_t n = (int64_t)chi * d;
   const int64_t nCh = (int64_t)chi * chi, nTe = (int64_t)chi * d * chi;
   int64_t p = std::min<int64_t>(n, chi + std::max(16, chi / 2));
@@ -199,6 +199,7 @@ MixedRun ctmrg_run_mixed(tnad_ctx* c, const double* a_, int d, int chi, double* 
   double best = std::numeric_limits<double>::infinity();
   int stall = 0;
   int counter = 0;
+  double judge_ref = 0.0;
   for (int k = 1;; ++k) {
     WsScope step(c);
     StepFwd f;
@@ -261,6 +262,11 @@ MixedRun ctmrg_run_mixed(tnad_ctx* c, const double* a_, int d, int chi, double* 
     run.last_diff = dv;
     counter++;
     if (counter > maxit) break;
+    if (judge && k == 2) judge_ref = dv;
+    if (judge && k == 4 && dv > tol && !(dv < judge_ref)) {
+      run.rejected = true;
+      break;
+    }
     if (prec == TNAD_PREC_FP64 || !ladder) {
       if (dv <= tol) break;
     } else {

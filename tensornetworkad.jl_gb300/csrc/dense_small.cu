@@ -7,6 +7,7 @@
 //    polishing steps; eigenvectors accumulate in global memory;
 //  - a counter-based Gaussian generator for deterministic start blocks.
 #include <cfloat>
+#include <atomic>
 #include <cmath>
 
 #include "tnad_internal.h"
@@ -14,24 +15,34 @@
 namespace tnad {
 
 // ---------------------------------------------------------------- Cholesky
-// G (p×p, column-major, symmetric positive definite) → Rinv (p×p) with
-// G = RᵀR, R upper triangular.  *fail = 1 when a pivot is not positive.
+// G (p×p, column-major, symmetric positive semi-definite) → Rinv (p×p) with
+// G + E = RᵀR, R upper triangular and E ≥ 0 diagonal: a pivot below
+// kPivotFloor·max_k G_kk (a column numerically inside the span of the previous
+// ones, e.g. when the subspace is wider than the rank of the matrix it
+// iterates on) is raised to that floor, so the factor stays finite and the
+// column maps to a vector of norm ≲ 1.  *fail = 1 when G has no positive
+// finite diagonal.
+constexpr double kPivotFloor = 1e-14;
+
 __global__ void k_chol_inv(const double* __restrict__ G, int p, double* __restrict__ Rinv, int* __restrict__ fail) {
   extern __shared__ double sm[];
   double* R = sm;  // p×p, column-major, upper triangle used
   for (int e = threadIdx.x; e < p * p; e += blockDim.x) R[e] = G[e];
   __syncthreads();
   __shared__ int bad;
-  if (threadIdx.x == 0) bad = 0;
+  __shared__ double floor_;
+  if (threadIdx.x == 0) {
+    double mx = 0.0;
+    for (int k = 0; k < p; ++k) mx = fmax(mx, R[k + k * p]);
+    bad = (mx > 0.0 && isfinite(mx)) ? 0 : 1;
+    floor_ = bad ? 1e-300 : kPivotFloor * mx;
+  }
   __syncthreads();
   // right-looking: for k, R[k,k] = sqrt(R[k,k]); R[k,j] /= R[k,k] (j>k); trailing update
   for (int k = 0; k < p; ++k) {
     if (threadIdx.x == 0) {
       double d = R[k + k * p];
-      if (!(d > 0.0)) {
-        bad = 1;
-        d = 1e-300;
-      }
+      if (!(d > floor_)) d = floor_;
       R[k + k * p] = sqrt(d);
     }
     __syncthreads();
@@ -60,7 +71,7 @@ __global__ void k_chol_inv(const double* __restrict__ G, int p, double* __restri
 void chol_inv_upper(tnad_ctx* c, const double* G, int64_t p, double* Rinv, int* dev_fail) {
   TNAD_REQUIRE(p >= 1 && p <= 160, TNAD_ERR_SHAPE, "chol_inv_upper: p must be in [1,160]");
   size_t sm = (size_t)p * p * 8;
-  static bool attr = false;
+  static std::atomic<bool> attr{false};
   if (!attr) {
     TNAD_CK(cudaFuncSetAttribute(k_chol_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 160 * 8));
     attr = true;
@@ -192,7 +203,7 @@ void eigh_small_prec(tnad_ctx* c, bool fp32, const double* A, int64_t p, double*
   WsScope scope(c);
   size_t sm = (size_t)(p + 1) * p * (fp32 ? 4 : 8);
   TNAD_REQUIRE(sm <= 200 * 1024, TNAD_ERR_SHAPE, "eigh_small: matrix does not fit in shared memory");
-  static bool attr32 = false, attr64 = false;
+  static std::atomic<bool> attr32{false}, attr64{false};
   if (fp32) {
     if (!attr32) {
       TNAD_CK(cudaFuncSetAttribute(k_eigh_jacobi<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
@@ -284,7 +295,7 @@ __global__ void k_polar_ns(const double* __restrict__ X, int m, int iters, doubl
 
 void polar_ns(tnad_ctx* c, const double* X, int64_t m, int iters, double* O, int* dev_info) {
   TNAD_REQUIRE(m >= 1 && m <= 128, TNAD_ERR_SHAPE, "polar_ns: m must be in [1,128]");
-  static bool attr = false;
+  static std::atomic<bool> attr{false};
   if (!attr) {
     TNAD_CK(cudaFuncSetAttribute(k_polar_ns, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 129 * 128 * 4));
     attr = true;

@@ -249,7 +249,19 @@ void energy_fwd(tnad_ctx* c, EnergyTape& tp, const double* h, const double* A, i
   double_layer(c, tp.As, D, s, tp.ap, tp.a);
   tp.C = P.d((int64_t)chi * chi);
   tp.T = P.d((int64_t)chi * d * chi);
-  if (o.warm_start && Cinit && Tinit) {
+  // starting environment: predicted by the attached network (vetted by the
+  // residual judge below), passed in by the caller, or :raw
+  bool learned = o.warm_start == TNAD_WARM_LEARNED;
+  c->warm_status = 0;
+  if (learned) {
+    TNAD_REQUIRE(c->warm_net && c->warm_D == D && c->warm_s == s && c->warm_chi == chi, TNAD_ERR_STATE,
+                 "energy: TNAD_WARM_LEARNED needs a network attached for this (D, s, χ)");
+    learned = warm_start_predict(c, c->warm_net, tp.As, (int)nA, chi, d, tp.C, tp.T);
+    if (!learned) {  // zero or non-finite prediction: rejected before any step
+      c->warm_status = -1;
+      init_raw_dev(c, tp.a, d, chi, tp.C, tp.T);
+    }
+  } else if (o.warm_start == TNAD_WARM_GIVEN && Cinit && Tinit) {
     copy_d2d(c, tp.C, Cinit, (int64_t)chi * chi);
     copy_d2d(c, tp.T, Tinit, (int64_t)chi * d * chi);
   } else {
@@ -263,8 +275,17 @@ void energy_fwd(tnad_ctx* c, EnergyTape& tp, const double* h, const double* A, i
   if (o.solver == TNAD_SOLVER_SUBSPACE) {
     // mixed precision + subspace solver; the implicit adjoint needs only x* and z*
     if (record) tp.zstar = P.d(n * chi);
-    MixedRun run = ctmrg_run_mixed(c, tp.a, d, chi, tp.C, tp.T, tol, maxit, o, record ? tp.zstar : nullptr);
-    tp.steps = run.steps;
+    MixedRun run = ctmrg_run_mixed(c, tp.a, d, chi, tp.C, tp.T, tol, maxit, o, record ? tp.zstar : nullptr, learned);
+    int probe = 0;
+    if (learned) {
+      c->warm_status = run.rejected ? -1 : 1;
+      if (run.rejected) {  // the residual did not fall: cold restart from :raw
+        probe = run.steps;
+        init_raw_dev(c, tp.a, d, chi, tp.C, tp.T);
+        run = ctmrg_run_mixed(c, tp.a, d, chi, tp.C, tp.T, tol, maxit, o, record ? tp.zstar : nullptr);
+      }
+    }
+    tp.steps = run.steps + probe;
     tp.fp64_steps = run.fp64_steps;
     tp.switch_step = run.switch_step;
     tp.last_diff = run.last_diff;
@@ -272,10 +293,22 @@ void energy_fwd(tnad_ctx* c, EnergyTape& tp, const double* h, const double* A, i
                  "energy: the subspace solver is differentiated with the fixed-point adjoint only");
   } else {
     const bool full_tape = record && o.adjoint == TNAD_ADJOINT_UNROLLED;
-    CtmrgRun run = ctmrg_run(c, o.prec == TNAD_PREC_FP64 ? TNAD_PREC_FP64 : TNAD_PREC_TF32X3, tp.a, d, chi, tp.C,
-                             tp.T, tol, maxit, (full_tape || record) ? &tp.ct : nullptr, &P,
-                             full_tape ? o.tape_budget : (int64_t)(2 * n * n + n) * 8 * (maxit + 2));
-    tp.steps = run.steps;
+    const int rprec = o.prec == TNAD_PREC_FP64 ? TNAD_PREC_FP64 : TNAD_PREC_TF32X3;
+    const int64_t budget = full_tape ? o.tape_budget : (int64_t)(2 * n * n + n) * 8 * (maxit + 2);
+    CtmrgRun run = ctmrg_run(c, rprec, tp.a, d, chi, tp.C, tp.T, tol, maxit, (full_tape || record) ? &tp.ct : nullptr,
+                             &P, budget, learned);
+    int probe = 0;
+    if (learned) {
+      c->warm_status = run.rejected ? -1 : 1;
+      if (run.rejected) {  // the residual did not fall: cold restart from :raw
+        probe = run.steps;
+        tp.ct = CtmrgTape();
+        init_raw_dev(c, tp.a, d, chi, tp.C, tp.T);
+        run = ctmrg_run(c, rprec, tp.a, d, chi, tp.C, tp.T, tol, maxit, (full_tape || record) ? &tp.ct : nullptr, &P,
+                        budget);
+      }
+    }
+    tp.steps = run.steps + probe;
     tp.last_diff = run.last_diff;
     if (record && o.adjoint == TNAD_ADJOINT_FIXEDPOINT) {
       TNAD_REQUIRE(!tp.ct.U.empty() && tp.ct.U.back(), TNAD_ERR_STATE, "energy: missing last projector");

@@ -15,10 +15,15 @@
 //                 tcgen05.commit; then all four warps drain TMEM (tcgen05.ld
 //                 32x32b, warp w owns lanes 32w..32w+31), apply alpha/beta and
 //                 store FP64 with coalesced column writes.
+// The same kernel, instantiated with SPLIT = false, is the BF16 GEMM of the
+// learned warm-start network: FP32 operands packed to one BF16 plane each,
+// one tcgen05.mma kind::f16 per 16-wide K step, FP32 accumulation and output.
 // Every mbarrier wait is bounded (~2 s of %globaltimer); on timeout the CTA
 // records an error, drains its own TMA loads (bounded), frees TMEM and exits,
 // and the host reports TNAD_ERR_TIMEOUT.
+#include <atomic>
 #include <cuda.h>
+#include <cuda_bf16.h>
 
 #include <cstring>
 #include <mutex>
@@ -29,14 +34,16 @@ namespace tnad {
 
 namespace {
 
-constexpr int BM = 128, BK = 32, STAGES = 3;
-constexpr int TILE_A = BM * BK * 4;  // 16 KiB per plane
+constexpr int BM = 128, BK = 32, STAGES = 3;  // BK: FP32 elements per 128-byte K slice
+constexpr int TILE_A = BM * 128;              // 16 KiB per plane (128 rows × 128 B)
 
-template <int BN>
+template <int BN, bool SPLIT>
 struct Cfg {
-  static constexpr int TILE_B = BN * BK * 4;
-  static constexpr int STAGE = 2 * TILE_A + 2 * TILE_B;
+  static constexpr int TILE_B = BN * 128;
+  static constexpr int PLANES = SPLIT ? 2 : 1;  // hi/lo planes per operand
+  static constexpr int STAGE = PLANES * (TILE_A + TILE_B);
   static constexpr int SMEM = STAGES * STAGE + 1024 + 256;
+  static constexpr int KSLICE = SPLIT ? 32 : 64;  // elements per 128-byte K slice (TF32 / BF16)
 };
 
 __device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -108,6 +115,15 @@ __device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t ad, uint64_t bd
       : "memory");
 }
 
+__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+      "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+      : "memory");
+}
+
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
@@ -118,13 +134,13 @@ __device__ __forceinline__ float tf32_rn(float x) {
   return __uint_as_float(r);
 }
 
-template <int BN>
+template <int BN, bool SPLIT, typename OutT>
 __global__ void __launch_bounds__(128, 1)
-    k_gemm_tf32x3(const __grid_constant__ CUtensorMap tAh, const __grid_constant__ CUtensorMap tAl,
-                  const __grid_constant__ CUtensorMap tBh, const __grid_constant__ CUtensorMap tBl, int M, int N,
-                  int kblocks_total, int kps, double alpha, double beta, double* __restrict__ C, int64_t ldc,
-                  double* __restrict__ P, int* err) {
-  using CF = Cfg<BN>;
+    k_gemm_tc(const __grid_constant__ CUtensorMap tAh, const __grid_constant__ CUtensorMap tAl,
+              const __grid_constant__ CUtensorMap tBh, const __grid_constant__ CUtensorMap tBl, int M, int N,
+              int kblocks_total, int kps, double alpha, double beta, OutT* __restrict__ C, int64_t ldc,
+              double* __restrict__ P, int* err) {
+  using CF = Cfg<BN, SPLIT>;
   // split-K: CTA z owns K slices [kbeg, kbeg + kblocks); with P != null it
   // writes its raw FP32 sum as an FP64 partial, reduced in FP64 afterwards
   const int kbeg = blockIdx.z * kps;
@@ -166,11 +182,16 @@ __global__ void __launch_bounds__(128, 1)
       uint8_t* st = smem + s * CF::STAGE;
       const uint32_t fb = full0 + 8 * s;
       mbar_expect_tx(fb, (uint32_t)CF::STAGE);
-      const int kx = (kbeg + kb) * BK;
-      tma_load_2d(su32(st), &tAh, kx, m0, fb);
-      tma_load_2d(su32(st + TILE_A), &tAl, kx, m0, fb);
-      tma_load_2d(su32(st + 2 * TILE_A), &tBh, kx, n0, fb);
-      tma_load_2d(su32(st + 2 * TILE_A + CF::TILE_B), &tBl, kx, n0, fb);
+      const int kx = (kbeg + kb) * CF::KSLICE;
+      if (SPLIT) {
+        tma_load_2d(su32(st), &tAh, kx, m0, fb);
+        tma_load_2d(su32(st + TILE_A), &tAl, kx, m0, fb);
+        tma_load_2d(su32(st + 2 * TILE_A), &tBh, kx, n0, fb);
+        tma_load_2d(su32(st + 2 * TILE_A + CF::TILE_B), &tBl, kx, n0, fb);
+      } else {
+        tma_load_2d(su32(st), &tAh, kx, m0, fb);
+        tma_load_2d(su32(st + TILE_A), &tBh, kx, n0, fb);
+      }
       issued = kb + 1;
     }
     // make sure none of this CTA's copies is still in flight when it exits
@@ -178,7 +199,9 @@ __global__ void __launch_bounds__(128, 1)
       mbar_wait(full0 + 8 * (kb % STAGES), (uint32_t)(kb / STAGES) & 1u, err, 2);
   } else if (warp == 1 && lane == 0) {
     // ---------------- MMA issuer ----------------
-    const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) |
+    // instruction descriptor: D = F32; A, B = TF32 (kind::tf32) or BF16 (kind::f16); both K-major
+    const uint32_t fmt = SPLIT ? 2u : 1u;
+    const uint32_t idesc = (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(BN >> 3) << 17) |
                            ((uint32_t)(BM >> 4) << 24);
     bool ok = true;
     for (int kb = 0; kb < kblocks && ok; ++kb) {
@@ -190,14 +213,23 @@ __global__ void __launch_bounds__(128, 1)
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t st = su32(smem + s * CF::STAGE);
-      const uint64_t ah = smem_desc(st), al = smem_desc(st + TILE_A);
-      const uint64_t bh = smem_desc(st + 2 * TILE_A), bl = smem_desc(st + 2 * TILE_A + CF::TILE_B);
+      if (SPLIT) {
+        const uint64_t ah = smem_desc(st), al = smem_desc(st + TILE_A);
+        const uint64_t bh = smem_desc(st + 2 * TILE_A), bl = smem_desc(st + 2 * TILE_A + CF::TILE_B);
 #pragma unroll
-      for (int k = 0; k < BK / 8; ++k) {
-        const uint64_t off = (uint64_t)((k * 8 * 4) >> 4);  // 32 bytes per 8-wide TF32 step
-        mma_tf32(tmem, ah + off, bh + off, idesc, (kb > 0 || k > 0) ? 1u : 0u);
-        mma_tf32(tmem, ah + off, bl + off, idesc, 1u);
-        mma_tf32(tmem, al + off, bh + off, idesc, 1u);
+        for (int k = 0; k < 4; ++k) {
+          const uint64_t off = (uint64_t)((k * 32) >> 4);  // 32 bytes per 8-wide TF32 step
+          mma_tf32(tmem, ah + off, bh + off, idesc, (kb > 0 || k > 0) ? 1u : 0u);
+          mma_tf32(tmem, ah + off, bl + off, idesc, 1u);
+          mma_tf32(tmem, al + off, bh + off, idesc, 1u);
+        }
+      } else {
+        const uint64_t ah = smem_desc(st), bh = smem_desc(st + TILE_A);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const uint64_t off = (uint64_t)((k * 32) >> 4);  // 32 bytes per 16-wide BF16 step
+          mma_bf16(tmem, ah + off, bh + off, idesc, (kb > 0 || k > 0) ? 1u : 0u);
+        }
       }
       mma_commit(empty0 + 8 * s);  // slot free once these MMAs have read it
     }
@@ -235,8 +267,8 @@ __global__ void __launch_bounds__(128, 1)
           const int col = n0 + c0 + j;
           if (col < N) {
             double r = alpha * (double)__uint_as_float(v[j]);
-            double* p = C + (int64_t)row + (int64_t)col * ldc;
-            *p = beta == 0.0 ? r : r + beta * (*p);
+            OutT* p = C + (int64_t)row + (int64_t)col * ldc;
+            *p = (OutT)(beta == 0.0 ? r : r + beta * (double)(*p));
           }
         }
       }
@@ -280,18 +312,39 @@ __global__ void k_pack_split(const double* __restrict__ X, int64_t ld, int tr, i
   }
 }
 
+// op(X) (rows × K, FP32 column-major) → one K-major BF16 plane, zero padded
+__global__ void k_pack_bf16(const float* __restrict__ X, int64_t ld, int tr, int64_t rows, int64_t K,
+                            int64_t rows_pad, int64_t k_pad, __nv_bfloat16* __restrict__ out) {
+  __shared__ float tile[32][33];
+  const int64_t r0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 × 8
+  for (int j = ty; j < 32; j += 8) {
+    int64_t r, k;
+    if (!tr) { r = r0 + tx; k = k0 + j; } else { k = k0 + tx; r = r0 + j; }
+    float v = 0.f;
+    if (r < rows && k < K) v = !tr ? X[r + k * ld] : X[k + r * ld];
+    if (!tr) tile[tx][j] = v; else tile[j][tx] = v;
+  }
+  __syncthreads();
+  for (int j = ty; j < 32; j += 8) {
+    const int64_t r = r0 + j, k = k0 + tx;
+    if (r < rows_pad && k < k_pad) out[r * k_pad + k] = __float2bfloat16_rn(tile[j][tx]);
+  }
+}
+
 constexpr int kChunkBlocks = 4;  // 4 × 32 = 128 K values per FP32 tensor-core accumulation
 
 // C = alpha·Σ_z P[z] + beta·C   (fixed order: deterministic)
+template <typename OutT>
 __global__ void k_splitk_sum(int64_t M, int64_t N, int splits, const double* __restrict__ P, double alpha,
-                             double beta, double* __restrict__ C, int64_t ldc) {
+                             double beta, OutT* __restrict__ C, int64_t ldc) {
   const int64_t MN = M * N;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < MN; e += (int64_t)gridDim.x * blockDim.x) {
     double s = 0.0;
     for (int z = 0; z < splits; ++z) s += P[e + z * MN];
     const int64_t i = e % M, j = e / M;
     const double r = alpha * s;
-    C[i + j * ldc] = beta == 0.0 ? r : r + beta * C[i + j * ldc];
+    C[i + j * ldc] = (OutT)(beta == 0.0 ? r : r + beta * (double)C[i + j * ldc]);
   }
 }
 
@@ -312,54 +365,57 @@ EncodeTiledFn encode_fn() {
   return fn;
 }
 
-CUtensorMap make_map(float* base, int64_t k_pad, int64_t rows_pad, int box_rows) {
+CUtensorMap make_map(void* base, int64_t k_pad, int64_t rows_pad, int box_rows, bool bf16) {
   CUtensorMap m;
   std::memset(&m, 0, sizeof(m));
   EncodeTiledFn fn = encode_fn();
   TNAD_REQUIRE(fn, TNAD_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
   cuuint64_t dims[2] = {(cuuint64_t)k_pad, (cuuint64_t)rows_pad};
-  cuuint64_t strides[1] = {(cuuint64_t)(k_pad * 4)};
-  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  const int esz = bf16 ? 2 : 4;
+  cuuint64_t strides[1] = {(cuuint64_t)(k_pad * esz)};
+  cuuint32_t box[2] = {(cuuint32_t)(128 / esz), (cuuint32_t)box_rows};  // one 128-byte K slice
   cuuint32_t es[2] = {1, 1};
-  CUresult r = fn(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, es,
+  CUresult r = fn(&m, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims,
+                  strides, box, es,
                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   TNAD_REQUIRE(r == CUDA_SUCCESS, TNAD_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
   return m;
 }
 
-template <int BN>
-void launch_tc(tnad_ctx* c, int64_t M, int64_t N, int64_t K, double alpha, const float* Ah, const float* Al,
-               const float* Bh, const float* Bl, int64_t Mp, int64_t Np, int64_t Kp, double beta, double* Cm,
-               int64_t ldc) {
-  static bool attr = false;
+template <int BN, bool SPLIT, typename OutT>
+void launch_tc(tnad_ctx* c, int64_t M, int64_t N, int64_t K, double alpha, void* Ah, void* Al, void* Bh, void* Bl,
+               int64_t Mp, int64_t Np, int64_t Kp, double beta, OutT* Cm, int64_t ldc, const char* timer_name) {
+  using CF = Cfg<BN, SPLIT>;
+  static std::atomic<bool> attr{false};
   if (!attr) {
-    TNAD_CK(cudaFuncSetAttribute(k_gemm_tf32x3<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg<BN>::SMEM));
+    TNAD_CK(cudaFuncSetAttribute(k_gemm_tc<BN, SPLIT, OutT>, cudaFuncAttributeMaxDynamicSharedMemorySize, CF::SMEM));
     attr = true;
   }
-  CUtensorMap tAh = make_map(const_cast<float*>(Ah), Kp, Mp, BM);
-  CUtensorMap tAl = make_map(const_cast<float*>(Al), Kp, Mp, BM);
-  CUtensorMap tBh = make_map(const_cast<float*>(Bh), Kp, Np, BN);
-  CUtensorMap tBl = make_map(const_cast<float*>(Bl), Kp, Np, BN);
+  CUtensorMap tAh = make_map(Ah, Kp, Mp, BM, !SPLIT);
+  CUtensorMap tBh = make_map(Bh, Kp, Np, BN, !SPLIT);
+  CUtensorMap tAl = SPLIT ? make_map(Al, Kp, Mp, BM, false) : tAh;
+  CUtensorMap tBl = SPLIT ? make_map(Bl, Kp, Np, BN, false) : tBh;
   // K is cut into chunks of ≤ kChunkBlocks slices; the tensor cores accumulate
   // each chunk in FP32 (error growing with the chunk length) and the chunks are
   // summed in FP64.  Chunks also multiply the CTA count of these short-K GEMMs.
-  const int kbt = (int)(Kp / BK);
-  const int splits = (kbt + kChunkBlocks - 1) / kChunkBlocks;
+  const int kbt = (int)(Kp / CF::KSLICE);
+  const int chunk = SPLIT ? kChunkBlocks : 2 * kChunkBlocks;
+  const int splits = (kbt + chunk - 1) / chunk;
   const int kps = (kbt + splits - 1) / splits;
   dim3 grid((unsigned)(Mp / BM), (unsigned)(Np / BN), (unsigned)splits);
   int* err = c->d_flag + 8;
   WsScope scope(c);
   double* P = splits > 1 ? ws_d(c, (int64_t)splits * M * N) : nullptr;
-  KernelTimer kt(c, "gemm_tf32x3", 2.0 * (double)M * (double)N * (double)K);  // logical FP64-equivalent flops
-  k_gemm_tf32x3<BN><<<grid, 128, Cfg<BN>::SMEM, c->stream>>>(tAh, tAl, tBh, tBl, (int)M, (int)N, kbt, kps, alpha,
-                                                             beta, Cm, ldc, P, err);
+  KernelTimer kt(c, timer_name, 2.0 * (double)M * (double)N * (double)K);  // logical flops
+  k_gemm_tc<BN, SPLIT, OutT><<<grid, 128, CF::SMEM, c->stream>>>(tAh, tAl, tBh, tBl, (int)M, (int)N, kbt, kps, alpha,
+                                                                 beta, Cm, ldc, P, err);
   count_launch(c);
-  check_launch(c, "gemm_tf32x3");
+  check_launch(c, timer_name);
   if (P) {
     const int64_t MN = M * N;
-    k_splitk_sum<<<(int)std::min<int64_t>((MN + 255) / 256, 4096), 256, 0, c->stream>>>(M, N, splits, P, alpha, beta,
-                                                                                      Cm, ldc);
+    k_splitk_sum<OutT><<<(int)std::min<int64_t>((MN + 255) / 256, 4096), 256, 0, c->stream>>>(M, N, splits, P,
+                                                                                            alpha, beta, Cm, ldc);
     count_launch(c);
     check_launch(c, "splitk_sum");
   }
@@ -399,9 +455,36 @@ void gemm_tf32x3(tnad_ctx* c, char ta, char tb, int64_t M, int64_t N, int64_t K,
   count_launch(c, 2);
   check_launch(c, "pack_split");
   if (BN == 128)
-    launch_tc<128>(c, M, N, K, alpha, Ah, Al, Bh, Bl, Mp, Np, Kp, beta, Cm, ldc);
+    launch_tc<128, true, double>(c, M, N, K, alpha, Ah, Al, Bh, Bl, Mp, Np, Kp, beta, Cm, ldc, "gemm_tf32x3");
   else
-    launch_tc<64>(c, M, N, K, alpha, Ah, Al, Bh, Bl, Mp, Np, Kp, beta, Cm, ldc);
+    launch_tc<64, true, double>(c, M, N, K, alpha, Ah, Al, Bh, Bl, Mp, Np, Kp, beta, Cm, ldc, "gemm_tf32x3");
+}
+
+void gemm_bf16(tnad_ctx* c, char ta, char tb, int64_t M, int64_t N, int64_t K, float alpha, const float* A,
+               int64_t lda, const float* B, int64_t ldb, float beta, float* Cm, int64_t ldc) {
+  if (M <= 0 || N <= 0) return;
+  TNAD_REQUIRE(c->tc_ok, TNAD_ERR_STATE, "BF16 GEMM needs an sm_100-family GPU (tcgen05)");
+  TNAD_REQUIRE(K > 0 && M < (1ll << 31) && N < (1ll << 31) && K < (1ll << 31), TNAD_ERR_ARG, "gemm_bf16: size");
+  const int BN = N > 64 ? 128 : 64;
+  const int64_t Mp = (M + BM - 1) / BM * BM, Np = (N + BN - 1) / BN * BN, Kp = (K + 63) / 64 * 64;
+  WsScope scope(c);
+  __nv_bfloat16* Ab = (__nv_bfloat16*)c->ws.alloc((size_t)Mp * Kp * 2);
+  __nv_bfloat16* Bb = (__nv_bfloat16*)c->ws.alloc((size_t)Np * Kp * 2);
+  const int ita = (ta == 'T' || ta == 't'), itb = (tb == 'T' || tb == 't');
+  {
+    dim3 g((unsigned)(Kp / 32), (unsigned)(Mp / 32)), b(32, 8);
+    k_pack_bf16<<<g, b, 0, c->stream>>>(A, lda, ita, M, K, Mp, Kp, Ab);
+  }
+  {
+    dim3 g((unsigned)(Kp / 32), (unsigned)(Np / 32)), b(32, 8);
+    k_pack_bf16<<<g, b, 0, c->stream>>>(B, ldb, itb ? 0 : 1, N, K, Np, Kp, Bb);
+  }
+  count_launch(c, 2);
+  check_launch(c, "pack_bf16");
+  if (BN == 128)
+    launch_tc<128, false, float>(c, M, N, K, alpha, Ab, nullptr, Bb, nullptr, Mp, Np, Kp, beta, Cm, ldc, "gemm_bf16");
+  else
+    launch_tc<64, false, float>(c, M, N, K, alpha, Ab, nullptr, Bb, nullptr, Mp, Np, Kp, beta, Cm, ldc, "gemm_bf16");
 }
 
 // Host check of the bounded-wait error flag (TNAD_ERR_TIMEOUT when a tensor-core

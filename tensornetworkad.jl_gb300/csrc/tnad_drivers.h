@@ -27,6 +27,7 @@ struct CtmrgTape {
 struct CtmrgRun {
   int steps = 0;
   double last_diff = 0.0;
+  bool rejected = false;  // judge: the residual did not fall from step 2 to step 4
 };
 
 // Intermediates of one step (workspace-backed).
@@ -64,7 +65,7 @@ void step_cache_fill(tnad_ctx* c, int prec, const double* a, int d, int chi, con
 // the result on exit.  With tape != null every step's input and decomposition
 // are recorded (pool owns the memory).
 CtmrgRun ctmrg_run(tnad_ctx* c, int prec, const double* a, int d, int chi, double* C, double* T, double tol,
-                   int maxit, CtmrgTape* tape, DevPool* pool, int64_t tape_budget);
+                   int maxit, CtmrgTape* tape, DevPool* pool, int64_t tape_budget, bool judge = false);
 // Reverse pass over a recorded CTMRG: dC/dT are the cotangents of the final
 // environment (overwritten as scratch); dbulk accumulates.
 void ctmrg_reverse(tnad_ctx* c, const CtmrgTape& tape, double* dC, double* dT, double* dbulk);

@@ -39,5 +39,10 @@ void expect_bwd(tnad_ctx* c, int prec, const double* h, int d, int s, int chi, c
 void energy_fwd(tnad_ctx* c, EnergyTape& tp, const double* h, const double* A, int D, int s, int chi, double tol,
                 int maxit, const tnad_opts& o, const double* Cinit, const double* Tinit, bool record);
 void energy_bwd(tnad_ctx* c, EnergyTape& tp, double dE, double* dA);
+// Learned warm start: (C, T) predicted by net for the symmetrised, normalised
+// site tensor As (n_in values), χ×χ and χ×d×χ on the device (mlp.cu); false
+// when the prediction is zero or not finite.
+bool warm_start_predict(tnad_ctx* c, tnad_mlp* net, const double* As, int n_in, int chi, int d, double* C,
+                        double* T);
 
 }  // namespace tnad

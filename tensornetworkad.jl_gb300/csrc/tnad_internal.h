@@ -87,6 +87,11 @@ struct tnad_ctx {
   std::string ktimer;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> kt_ev;
   double kt_work = 0.0;
+  // learned warm start (tnad_ctx_set_warm_start): network, the (D, s, χ) it
+  // was trained for, and the outcome of the last energy call that used it
+  tnad_mlp* warm_net = nullptr;
+  int warm_D = 0, warm_s = 0, warm_chi = 0;
+  int warm_status = 0;
 };
 
 namespace tnad {
@@ -173,6 +178,10 @@ void gemm_f64(tnad_ctx* c, char ta, char tb, int64_t M, int64_t N, int64_t K, do
 void gemm_tf32x3(tnad_ctx* c, char ta, char tb, int64_t M, int64_t N, int64_t K, double alpha,
                  const double* A, int64_t lda, const double* B, int64_t ldb, double beta,
                  double* C, int64_t ldc);
+// FP32 C(M×N) = alpha·op(A)·op(B) + beta·C with operands rounded to BF16 and FP32
+// accumulation on tcgen05 tensor cores (chunks of 512 K values summed in FP64).
+void gemm_bf16(tnad_ctx* c, char ta, char tb, int64_t M, int64_t N, int64_t K, float alpha, const float* A,
+               int64_t lda, const float* B, int64_t ldb, float beta, float* C, int64_t ldc);
 // Raises TNAD_ERR_TIMEOUT if a tensor-core GEMM gave up on a bounded wait (syncs).
 void check_tc_errors(tnad_ctx* c);
 void gemm(tnad_ctx* c, int prec, char ta, char tb, int64_t M, int64_t N, int64_t K, double alpha,

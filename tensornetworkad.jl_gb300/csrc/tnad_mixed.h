@@ -14,15 +14,18 @@ struct MixedRun {
   int switch_step = 0;  // step at which the ladder handed over to FP64 (0: never)
   int power_steps = 0;  // M·Q products in total
   double last_diff = std::numeric_limits<double>::infinity();
+  bool rejected = false;  // judge: the residual did not fall from step 2 to step 4
 };
 
 // z (n×χ) ← z·polar(zᵀ·zprev) (orthogonal Procrustes gauge alignment)
 void align_polar(tnad_ctx* c, int prec, double* z, const double* zprev, int64_t n, int chi);
 
 // C/T: initial environment in, converged environment out.  zfinal (n×χ, may be
-// null) receives the projector of the last step.
+// null) receives the projector of the last step.  With judge set the run stops
+// at step 4 with rejected = true unless its residual fell below that of step 2
+// (used to vet a predicted starting environment).
 MixedRun ctmrg_run_mixed(tnad_ctx* c, const double* a, int d, int chi, double* C, double* T, double tol, int maxit,
-                         const tnad_opts& o, double* zfinal);
+                         const tnad_opts& o, double* zfinal, bool judge = false);
 
 struct FixedPointInfo {
   int iters = 0;

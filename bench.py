@@ -51,6 +51,9 @@ def parse():
     p.add_argument("--n-held", dest="n_held", type=int, default=500, help="held-out tensors")
     p.add_argument("--train-steps", dest="train_steps", type=int, default=6000)
     p.add_argument("--threads", type=int, default=8, help="concurrent CTMRG runs while generating targets")
+    p.add_argument("--profile", default=None, choices=["solve", "mlp"],
+                   help="run one untimed solve of the workload (solve) or 20 training steps of the D=3, chi=36 "
+                        "warm-start network (mlp) and exit: the command profiled by ncu")
     return p.parse_args()
 
 
@@ -121,12 +124,13 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def dist_init(n):
+def dist_init(n, backend="nccl"):
+    """One process per GPU (torchrun env); every rank solves its own replica."""
     if n <= 1:
         return None, 0, 1
     import torch.distributed as dist
 
-    dist.init_process_group("nccl")
+    dist.init_process_group(backend)
     return dist, dist.get_rank(), dist.get_world_size()
 
 
@@ -135,7 +139,8 @@ def max_over_ranks(dist, x):
         return x
     import torch
 
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -455,9 +460,33 @@ def run_learned(args):
     print(json.dumps(line), flush=True)
 
 
+def run_profile(args):
+    import importlib
+
+    import __graft_entry__ as ge
+
+    tn = ge.load_package()
+    if args.profile == "solve":
+        E, st = Solver(tn, ESTAR[args.workload], args.mode).device()
+        print(f"profile solve: E={E!r} steps={st['steps']} launches={tn.ctx().launches}", flush=True)
+        return
+    wl = importlib.import_module(tn.__name__ + ".learned")
+    net = wl.WarmStartNet(3, 2, 36, width=512, seed=1)
+    rng = np.random.default_rng(0)
+    X = rng.standard_normal((net.n_in, 1024)).astype(np.float32)
+    Y = rng.standard_normal((net.n_out, 1024)).astype(np.float32)
+    net.set_data(X, Y)
+    loss = None
+    for k in range(20):
+        loss = net.train_step(rng.integers(0, 1024, 128), 1e-3, 1e-4, want_loss=(k == 19))
+    print(f"profile mlp: 20 AdamW steps, batch 128, loss={loss:.4f} launches={tn.ctx().launches}", flush=True)
+
+
 if __name__ == "__main__":
     a = parse()
-    if a.impl == "reference":
+    if a.profile:
+        run_profile(a)
+    elif a.impl == "reference":
         run_reference(a)
     elif a.workload.startswith("learned"):
         run_learned(a)

@@ -249,6 +249,21 @@ def heisenberg_trajectory(D: int, chi: int, Jz: float, rng: np.random.Generator,
     return seen[:evals]
 
 
+def shard_range(n: int, rank: int, world: int) -> range:
+    """Contiguous share of n independent units (site tensors) for one rank."""
+    lo = n * rank // world
+    return range(lo, n * (rank + 1) // world)
+
+
+def gather_shards(part: list, dist=None) -> list:
+    """Concatenate every rank's share in rank order (identity without a process group)."""
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return list(part)
+    parts = [None] * dist.get_world_size()
+    dist.all_gather_object(parts, list(part))
+    return [x for p in parts for x in p]
+
+
 def stack(samples: list[Sample]):
     X = np.stack([s.x for s in samples], axis=1).astype(np.float32)
     Y = np.stack([s.y for s in samples], axis=1).astype(np.float32)

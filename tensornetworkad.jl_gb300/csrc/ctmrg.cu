@@ -153,7 +153,7 @@ void ctmrg_step_fwd(tnad_ctx* c, int prec, const double* a_, int d, int chi, con
   // cpmat = reshape(cp, χD, χD); cpmat += cpmat'; u,s,v = svd(cpmat)   (:134-136)
   f.M = ws_d(c, n * n);
   add_transpose(c, n, f.cp.p, f.M);
-  svd_jacobi(c, f.M, n, n, U, S, V, true);
+  svd_jacobi(c, f.M, n, n, U, S, V, true, 0);
   Ten z = make_ten(U, {chi, d, chi});  // z = reshape(u[:, 1:χ], χ, D, χ)  (:137)
   project(c, prec, a, T, z, f);
   if (vals) {

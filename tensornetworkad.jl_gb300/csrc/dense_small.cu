@@ -15,69 +15,97 @@
 namespace tnad {
 
 // ---------------------------------------------------------------- Cholesky
-// G (p×p, column-major, symmetric positive semi-definite) → Rinv (p×p) with
-// G + E = RᵀR, R upper triangular and E ≥ 0 diagonal: a pivot below
+// G (p×p, column-major, symmetric positive semi-definite) → R (p×p, upper
+// triangular, zeros below) with G + E = RᵀR and E ≥ 0 diagonal: a pivot below
 // kPivotFloor·max_k G_kk (a column numerically inside the span of the previous
 // ones, e.g. when the subspace is wider than the rank of the matrix it
 // iterates on) is raised to that floor, so the factor stays finite and the
 // column maps to a vector of norm ≲ 1.  *fail = 1 when G has no positive
-// finite diagonal.
+// finite diagonal.  One CTA, right-looking, the matrix in shared memory.
 constexpr double kPivotFloor = 1e-14;
 
-__global__ void k_chol_inv(const double* __restrict__ G, int p, double* __restrict__ Rinv, int* __restrict__ fail) {
+__global__ void k_chol_factor(const double* __restrict__ G, int p, double* __restrict__ Rg, int* __restrict__ fail) {
   extern __shared__ double sm[];
-  double* R = sm;  // p×p, column-major, upper triangle used
-  for (int e = threadIdx.x; e < p * p; e += blockDim.x) R[e] = G[e];
+  const int ld = p + 1;  // padded: row accesses R[k, i..] hit distinct banks
+  double* R = sm;        // p × ld, column-major, upper triangle used
+  for (int e = threadIdx.x; e < p * p; e += blockDim.x) R[(e % p) + (e / p) * ld] = G[e];
   __syncthreads();
   __shared__ int bad;
   __shared__ double floor_;
   if (threadIdx.x == 0) {
     double mx = 0.0;
-    for (int k = 0; k < p; ++k) mx = fmax(mx, R[k + k * p]);
+    for (int k = 0; k < p; ++k) mx = fmax(mx, R[k + k * ld]);
     bad = (mx > 0.0 && isfinite(mx)) ? 0 : 1;
     floor_ = bad ? 1e-300 : kPivotFloor * mx;
   }
   __syncthreads();
-  // right-looking: for k, R[k,k] = sqrt(R[k,k]); R[k,j] /= R[k,k] (j>k); trailing update
+  // for k: R[k,k] = sqrt(R[k,k]); R[k,j] /= R[k,k] (j>k); trailing update
   for (int k = 0; k < p; ++k) {
-    if (threadIdx.x == 0) {
-      double d = R[k + k * p];
-      if (!(d > floor_)) d = floor_;
-      R[k + k * p] = sqrt(d);
-    }
+    double d = R[k + k * ld];
+    if (!(d > floor_)) d = floor_;
+    const double rkk = sqrt(d);
     __syncthreads();
-    const double rkk = R[k + k * p];
-    for (int j = k + 1 + threadIdx.x; j < p; j += blockDim.x) R[k + j * p] /= rkk;
+    if (threadIdx.x == 0) R[k + k * ld] = rkk;
+    const double inv = 1.0 / rkk;
+    for (int j = k + 1 + threadIdx.x; j < p; j += blockDim.x) R[k + j * ld] *= inv;
     __syncthreads();
     // trailing update of the upper triangle: R[i,j] -= R[k,i]·R[k,j] for k<i<=j
     const int m = p - k - 1;
     for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
       const int i = k + 1 + e % m, j = k + 1 + e / m;
-      if (i <= j) R[i + j * p] -= R[k + i * p] * R[k + j * p];
+      if (i <= j) R[i + j * ld] -= R[k + i * ld] * R[k + j * ld];
     }
     __syncthreads();
   }
-  // inverse of the upper-triangular R: column j of X solves R·x = e_j (back substitution)
-  for (int j = threadIdx.x; j < p; j += blockDim.x) {
-    for (int i = p - 1; i >= 0; --i) {
-      double s = (i == j) ? 1.0 : 0.0;
-      for (int l = i + 1; l <= j; ++l) s -= R[i + l * p] * Rinv[l + (int64_t)j * p];
-      Rinv[i + (int64_t)j * p] = (i <= j) ? s / R[i + i * p] : 0.0;
-    }
+  for (int e = threadIdx.x; e < p * p; e += blockDim.x) {
+    const int i = e % p, j = e / p;
+    Rg[e] = i <= j ? R[i + j * ld] : 0.0;
   }
   if (threadIdx.x == 0 && bad) *fail = 1;
 }
 
+// Rinv = R⁻¹ for upper-triangular R (p×p): one warp per column j solves
+// R·x = e_j by back substitution (lanes split each row's dot product), R in
+// shared memory with leading dimension p+1; 8 columns per CTA.
+__global__ void k_tri_inv(const double* __restrict__ Rg, int p, double* __restrict__ Rinv) {
+  extern __shared__ double sm[];
+  const int ld = p + 1;
+  double* R = sm;              // p × ld
+  double* rd = sm + p * ld;    // 1/R[i,i]
+  double* X = rd + p;          // 8 × p solution columns
+  for (int e = threadIdx.x; e < p * p; e += blockDim.x) {
+    const int i = e % p, j = e / p;
+    R[i + j * ld] = Rg[e];
+  }
+  for (int i = threadIdx.x; i < p; i += blockDim.x) rd[i] = 1.0 / Rg[i + (int64_t)i * p];
+  __syncthreads();
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int j = blockIdx.x * 8 + w;
+  if (j >= p) return;
+  double* x = X + w * p;
+  for (int i = j; i >= 0; --i) {
+    double s = 0.0;
+    for (int l = i + 1 + lane; l <= j; l += 32) s += R[i + l * ld] * x[l];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) x[i] = ((i == j ? 1.0 : 0.0) - s) * rd[i];
+    __syncwarp();
+  }
+  for (int i = lane; i < p; i += 32) Rinv[i + (int64_t)j * p] = i <= j ? x[i] : 0.0;
+}
+
 void chol_inv_upper(tnad_ctx* c, const double* G, int64_t p, double* Rinv, int* dev_fail) {
   TNAD_REQUIRE(p >= 1 && p <= 160, TNAD_ERR_SHAPE, "chol_inv_upper: p must be in [1,160]");
-  size_t sm = (size_t)p * p * 8;
   static std::atomic<bool> attr{false};
   if (!attr) {
-    TNAD_CK(cudaFuncSetAttribute(k_chol_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 160 * 8));
+    TNAD_CK(cudaFuncSetAttribute(k_chol_factor, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 161 * 8));
+    TNAD_CK(cudaFuncSetAttribute(k_tri_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (160 * 161 + 9 * 160) * 8));
     attr = true;
   }
-  k_chol_inv<<<1, 256, sm, c->stream>>>(G, (int)p, Rinv, dev_fail);
-  count_launch(c);
+  WsScope scope(c);
+  double* R = ws_d(c, p * p);
+  k_chol_factor<<<1, 256, (size_t)p * (p + 1) * 8, c->stream>>>(G, (int)p, R, dev_fail);
+  k_tri_inv<<<(unsigned)((p + 7) / 8), 256, (size_t)(p * (p + 1) + 9 * p) * 8, c->stream>>>(R, (int)p, Rinv);
+  count_launch(c, 2);
   check_launch(c, "chol_inv");
 }
 
@@ -104,13 +132,26 @@ __global__ void k_eigh_jacobi(const double* __restrict__ A, int p, int max_sweep
   __shared__ T cs_[128], sn_[128];
   __shared__ int pp_[128], qq_[128];
   __shared__ int rotated;
+  __shared__ double fro_part[32];
   const int NP = p + (p & 1);
-  const T tol = (T)(sizeof(T) == 8 ? 4.0 * DBL_EPSILON : 4.0 * FLT_EPSILON) * (T)sqrt((double)p);
+  const double eps_t = sizeof(T) == 8 ? DBL_EPSILON : FLT_EPSILON;
+  const T tol = (T)(4.0 * eps_t * sqrt((double)p));
+  double ss = 0.0;
   for (int e = threadIdx.x; e < p * p; e += blockDim.x) {
-    H[(e % p) + (e / p) * ld] = (T)A[e];
+    const double v = A[e];
+    ss += v * v;
+    H[(e % p) + (e / p) * ld] = (T)v;
     Z[e] = (e % p == e / p) ? (T)1 : (T)0;
   }
+  for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+  if ((threadIdx.x & 31) == 0) fro_part[threadIdx.x >> 5] = ss;
   __syncthreads();
+  // Rounding floor of the stop rule: every rotation leaves noise of size
+  // ~ε·‖H‖ in the off-diagonal entries of small eigenvalues, which a purely
+  // relative rule would keep rotating until the sweep cap.
+  double fro2 = 0.0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) fro2 += fro_part[w];
+  const T absfl = (T)(2.0 * eps_t * sqrt((double)p) * sqrt(fro2));
   int sweep = 0;
   for (; sweep < max_sweeps; ++sweep) {
     if (threadIdx.x == 0) rotated = 0;
@@ -129,7 +170,7 @@ __global__ void k_eigh_jacobi(const double* __restrict__ A, int p, int max_sweep
           }
           const T apq = H[a + b * ld], app = H[a + a * ld], aqq = H[b + b * ld];
           if (apq != (T)0 && fabs((double)apq) > (double)tol * sqrt(fabs((double)app * (double)aqq)) &&
-              fabs((double)apq) > 1e-300) {
+              fabs((double)apq) > (double)absfl && fabs((double)apq) > 1e-300) {
             const T tau = (aqq - app) / ((T)2 * apq);
             const T t = (tau >= (T)0 ? (T)1 : (T)-1) / (fabs(tau) + sqrt((T)1 + tau * tau));
             c = (T)1 / sqrt((T)1 + t * t);
@@ -201,19 +242,21 @@ void eigh_small_prec(tnad_ctx* c, bool fp32, const double* A, int64_t p, double*
                      int* dev_info) {
   TNAD_REQUIRE(p >= 1 && p <= 256, TNAD_ERR_SHAPE, "eigh_small: p must be in [1,256]");
   WsScope scope(c);
-  size_t sm = (size_t)(p + 1) * p * (fp32 ? 4 : 8);
-  TNAD_REQUIRE(sm <= 200 * 1024, TNAD_ERR_SHAPE, "eigh_small: matrix does not fit in shared memory");
+  const size_t sm = (size_t)(p + 1) * p * (fp32 ? 4 : 8);
+  const size_t kMaxSm = 200 * 1024;
+  TNAD_REQUIRE(sm <= kMaxSm, TNAD_ERR_SHAPE, "eigh_small: matrix does not fit in shared memory");
   static std::atomic<bool> attr32{false}, attr64{false};
+  // eigenvectors accumulate in global memory (L1-cached); H lives in shared memory
   if (fp32) {
     if (!attr32) {
-      TNAD_CK(cudaFuncSetAttribute(k_eigh_jacobi<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+      TNAD_CK(cudaFuncSetAttribute(k_eigh_jacobi<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSm));
       attr32 = true;
     }
     float* Z = ws_f(c, p * p);
     k_eigh_jacobi<float><<<1, 512, sm, c->stream>>>(A, (int)p, max_sweeps, lam, W, Z, dev_info);
   } else {
     if (!attr64) {
-      TNAD_CK(cudaFuncSetAttribute(k_eigh_jacobi<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+      TNAD_CK(cudaFuncSetAttribute(k_eigh_jacobi<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSm));
       attr64 = true;
     }
     double* Z = ws_d(c, p * p);

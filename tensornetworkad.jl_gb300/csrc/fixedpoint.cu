@@ -150,7 +150,7 @@ FixedPointInfo ctmrg_fixedpoint_adjoint(tnad_ctx* c, int prec, const double* a_,
     grow(c, TNAD_PREC_FP64, a, C, T, f);
     double* M = ws_d(c, n * n);
     add_transpose(c, n, f.cp.p, M);
-    svd_jacobi(c, M, n, n, U, S, V, true);
+    svd_jacobi(c, M, n, n, U, S, V, true, 0);
   }
   tr.mark("gauge");
   double* X = ws_d(c, (int64_t)chi * chi);

@@ -17,7 +17,9 @@
 namespace tnad {
 
 static const int kMaxSweeps = 100;
-static const int kRelSweeps = 20;
+static const int kRelSweeps = 20;  // relative-rule sweeps of the general (non-symmetric) SVD
+static const int kMaxSweeps32 = 30;  // FP32 preconditioning sweeps (symmetric A)
+static const int64_t kPrecondMinN = 256;  // smaller matrices skip the FP32 preconditioning
 
 __device__ __forceinline__ double wsum(double v) {
 #pragma unroll
@@ -92,13 +94,22 @@ __global__ void k_jacobi_round(double* __restrict__ W, double* __restrict__ V, i
 
 // Same round with one 128-thread CTA per column pair: each thread keeps R rows
 // of both columns in registers (one read and one write of W per round), the
-// three dot products reduce through warp shuffles and shared memory.
-template <int R>
-__global__ void __launch_bounds__(128) k_jacobi_round_cta(double* __restrict__ W, double* __restrict__ V, int64_t m,
+// three dot products reduce through warp shuffles and shared memory.  T is
+// double for the decomposition itself and float for the preconditioning sweeps
+// (rotation angles are always formed in FP64).
+template <typename T>
+__device__ __forceinline__ T wsum_t(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <int R, typename T>
+__global__ void __launch_bounds__(128) k_jacobi_round_cta(T* __restrict__ W, T* __restrict__ V, int64_t m,
                                                           int64_t n, int r, int NP, double tol, double abs_eps,
                                                           const double* __restrict__ fro2, int* __restrict__ rotated) {
-  __shared__ double red[3][4];
-  __shared__ double rot[2];
+  __shared__ T red[3][4];
+  __shared__ T rot[2];
   int p, q;
   pair_of(r, blockIdx.x, NP, &p, &q);
   if (p >= n || q >= n) return;  // bye (uniform across the CTA)
@@ -107,15 +118,15 @@ __global__ void __launch_bounds__(128) k_jacobi_round_cta(double* __restrict__ W
     p = q;
     q = t;
   }
-  double* wp = W + (int64_t)p * m;
-  double* wq = W + (int64_t)q * m;
-  double x[R], y[R];
-  double a = 0.0, b = 0.0, g = 0.0;
+  T* wp = W + (int64_t)p * m;
+  T* wq = W + (int64_t)q * m;
+  T x[R], y[R];
+  T a = 0, b = 0, g = 0;
 #pragma unroll
   for (int k = 0; k < R; ++k) {
     const int64_t i = threadIdx.x + (int64_t)k * 128;
-    x[k] = i < m ? wp[i] : 0.0;
-    y[k] = i < m ? wq[i] : 0.0;
+    x[k] = i < m ? wp[i] : (T)0;
+    y[k] = i < m ? wq[i] : (T)0;
   }
 #pragma unroll
   for (int k = 0; k < R; ++k) {
@@ -123,9 +134,9 @@ __global__ void __launch_bounds__(128) k_jacobi_round_cta(double* __restrict__ W
     b = fma(y[k], y[k], b);
     g = fma(x[k], y[k], g);
   }
-  a = wsum(a);
-  b = wsum(b);
-  g = wsum(g);
+  a = wsum_t(a);
+  b = wsum_t(b);
+  g = wsum_t(g);
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (lane == 0) {
     red[0][w] = a;
@@ -134,24 +145,24 @@ __global__ void __launch_bounds__(128) k_jacobi_round_cta(double* __restrict__ W
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    a = red[0][0] + red[0][1] + red[0][2] + red[0][3];
-    b = red[1][0] + red[1][1] + red[1][2] + red[1][3];
-    g = red[2][0] + red[2][1] + red[2][2] + red[2][3];
+    const double A = (double)red[0][0] + red[0][1] + red[0][2] + red[0][3];
+    const double B = (double)red[1][0] + red[1][1] + red[1][2] + red[1][3];
+    const double G = (double)red[2][0] + red[2][1] + red[2][2] + red[2][3];
     double cs = 1.0, sn = 0.0;
-    if (g != 0.0 && a != 0.0 && b != 0.0 &&
-        fabs(g) > tol * sqrt(a) * sqrt(b) + abs_eps * sqrt(fro2[0]) * (sqrt(a) + sqrt(b))) {
-      const double zeta = (b - a) / (2.0 * g);
+    if (G != 0.0 && A != 0.0 && B != 0.0 &&
+        fabs(G) > tol * sqrt(A) * sqrt(B) + abs_eps * sqrt(fro2[0]) * (sqrt(A) + sqrt(B))) {
+      const double zeta = (B - A) / (2.0 * G);
       const double t = fabs(zeta) > 1e150 ? 0.5 / zeta : copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
       cs = 1.0 / sqrt(1.0 + t * t);
       sn = cs * t;
       atomicAdd(rotated, 1);
     }
-    rot[0] = cs;
-    rot[1] = sn;
+    rot[0] = (T)cs;
+    rot[1] = (T)sn;
   }
   __syncthreads();
-  const double cs = rot[0], sn = rot[1];
-  if (sn == 0.0) return;
+  const T cs = rot[0], sn = rot[1];
+  if (sn == (T)0) return;
 #pragma unroll
   for (int k = 0; k < R; ++k) {
     const int64_t i = threadIdx.x + (int64_t)k * 128;
@@ -160,13 +171,91 @@ __global__ void __launch_bounds__(128) k_jacobi_round_cta(double* __restrict__ W
       wq[i] = sn * x[k] + cs * y[k];
     }
   }
-  double* vp = V + (int64_t)p * n;
-  double* vq = V + (int64_t)q * n;
+  T* vp = V + (int64_t)p * n;
+  T* vq = V + (int64_t)q * n;
   for (int64_t i = threadIdx.x; i < n; i += 128) {
-    const double xv = vp[i], yv = vq[i];
+    const T xv = vp[i], yv = vq[i];
     vp[i] = cs * xv - sn * yv;
     vq[i] = sn * xv + cs * yv;
   }
+}
+
+// one round over all column pairs (T = double or float)
+template <typename T>
+void jacobi_round_launch(tnad_ctx* c, T* W, T* V, int64_t m, int64_t n, int r, int NP, double tol, double ae,
+                         const double* fro2, int* flag) {
+  const unsigned np2 = (unsigned)(NP / 2);
+  if (m <= 256)
+    k_jacobi_round_cta<2, T><<<np2, 128, 0, c->stream>>>(W, V, m, n, r, NP, tol, ae, fro2, flag);
+  else if (m <= 512)
+    k_jacobi_round_cta<4, T><<<np2, 128, 0, c->stream>>>(W, V, m, n, r, NP, tol, ae, fro2, flag);
+  else if (m <= 1024)
+    k_jacobi_round_cta<8, T><<<np2, 128, 0, c->stream>>>(W, V, m, n, r, NP, tol, ae, fro2, flag);
+  else
+    k_jacobi_round_cta<16, T><<<np2, 128, 0, c->stream>>>(W, V, m, n, r, NP, tol, ae, fro2, flag);
+}
+
+// One Jacobi sweep (flag reset + the NP−1 rounds) recorded once as a CUDA
+// graph and replayed for every sweep: the rounds are short kernels whose
+// launch cost is comparable to their run time.  Sweeps bracketed by the kernel
+// timer (event records cannot go into the graph) and very small matrices are
+// launched directly.
+template <typename T>
+struct SweepGraph {
+  cudaGraphExec_t exec = nullptr;
+  double ae_ = -1.0;
+  ~SweepGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+  void run(tnad_ctx* c, const char* family, T* W, T* V, int64_t m, int64_t n, int NP, double tol, double ae,
+           const double* fro2, int* flag, double round_flops) {
+    const bool timed = !c->ktimer.empty() && c->ktimer == family;
+    if (timed || NP < 64) {
+      TNAD_CK(cudaMemsetAsync(flag, 0, sizeof(int), c->stream));
+      for (int r = 0; r < NP - 1; ++r) {
+        KernelTimer kt(c, family, round_flops);
+        jacobi_round_launch<T>(c, W, V, m, n, r, NP, tol, ae, fro2, flag);
+      }
+    } else {
+      if (exec && ae != ae_) {
+        TNAD_CK(cudaGraphExecDestroy(exec));
+        exec = nullptr;
+      }
+      if (!exec) {
+        cudaGraph_t g = nullptr;
+        TNAD_CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int), c->stream);
+        for (int r = 0; r < NP - 1 && e == cudaSuccess; ++r) {
+          jacobi_round_launch<T>(c, W, V, m, n, r, NP, tol, ae, fro2, flag);
+          e = cudaGetLastError();
+        }
+        const cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+        if (e == cudaSuccess) e = e2;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (e != cudaSuccess) fail(TNAD_ERR_CUDA, std::string("jacobi sweep graph: ") + cudaGetErrorString(e));
+        ae_ = ae;
+      }
+      TNAD_CK(cudaGraphLaunch(exec, c->stream));
+    }
+    count_launch(c, NP - 1);
+    check_launch(c, family);
+  }
+};
+
+__global__ void k_to_float(const double* __restrict__ x, int64_t n, float* __restrict__ y) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+    y[e] = (float)x[e];
+}
+
+__global__ void k_to_double(const float* __restrict__ x, int64_t n, double* __restrict__ y) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+    y[e] = (double)x[e];
+}
+
+__global__ void k_eye_f(float* V, int64_t n) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n * n; e += (int64_t)gridDim.x * blockDim.x)
+    V[e] = (e % n == e / n) ? 1.f : 0.f;
 }
 
 __global__ void k_eye(double* V, int64_t n) {
@@ -320,7 +409,7 @@ __global__ void k_complete_col(double* __restrict__ U, int64_t m, int64_t k, dou
 }
 
 void svd_jacobi(tnad_ctx* c, const double* A, int64_t m, int64_t n, double* U, double* S, double* V,
-                bool symmetric) {
+                bool symmetric, int rel_sweeps) {
   TNAD_REQUIRE(m >= n && n >= 1, TNAD_ERR_SHAPE, "svd_jacobi: needs m >= n >= 1");
   WsScope scope(c);
   double* W = ws_d(c, m * n);
@@ -350,33 +439,62 @@ void svd_jacobi(tnad_ctx* c, const double* A, int64_t m, int64_t n, double* U, d
   bool converged = (n == 1);
   const int threads = 256;
   const int blocks = (NP / 2 * 32 + threads - 1) / threads;
+  const int64_t nb_nn = std::min<int64_t>((n * n + 255) / 256, 4096);
+  if (symmetric && n >= kPrecondMinN && m <= 2048 && !converged) {
+    // FP32 preconditioning: Jacobi sweeps on a float copy (the FP32 pipe is
+    // much wider than the FP64 one) until rotations stop at FP32 accuracy; the
+    // accumulated V32 is re-orthogonalised in FP64 (Newton–Schulz) and the FP64
+    // sweeps below start from W = A·V, whose columns are then orthogonal to
+    // ~1e-5: the FP64 phase needs a few sweeps instead of ~20.
+    float* W32 = ws_f(c, m * n);
+    float* V32 = ws_f(c, n * n);
+    k_to_float<<<(int)std::min<int64_t>((m * n + 255) / 256, 4096), 256, 0, c->stream>>>(A, m * n, W32);
+    k_eye_f<<<(int)nb_nn, 256, 0, c->stream>>>(V32, n);
+    count_launch(c, 2);
+    const double tol32 = 4.0 * std::sqrt((double)m) * FLT_EPSILON, ae32 = 2.0 * FLT_EPSILON;
+    SweepGraph<float> sweep32;
+    const double round_flops = (double)(n / 2) * (12.0 * (double)m + 6.0 * (double)n);
+    for (int sweep = 0; sweep < kMaxSweeps32; ++sweep) {
+      sweep32.run(c, "jacobi_round_f32", W32, V32, m, n, NP, tol32, ae32, fro2, flag, round_flops);
+      TNAD_CK(cudaMemcpyAsync(c->h_flag, flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+      TNAD_CK(cudaStreamSynchronize(c->stream));
+      if (c->h_flag[0] <= (int)(n / 64)) break;  // a few stragglers are left to FP64
+    }
+    k_to_double<<<(int)nb_nn, 256, 0, c->stream>>>(V32, n * n, Vw);
+    count_launch(c);
+    // V ← V·(3I − VᵀV)/2, three times: orthogonal to FP64 rounding
+    double* G = ws_d(c, n * n);
+    double* V2 = ws_d(c, n * n);
+    for (int it = 0; it < 3; ++it) {
+      gemm_f64(c, 'T', 'N', n, n, n, 1.0, Vw, n, Vw, n, 0.0, G, n);
+      copy_d2d(c, V2, Vw, n * n);
+      gemm_f64(c, 'N', 'N', n, n, n, -0.5, Vw, n, G, n, 1.5, V2, n);
+      copy_d2d(c, Vw, V2, n * n);
+    }
+    gemm_f64(c, 'N', 'N', m, n, n, 1.0, A, m, Vw, n, 0.0, W, m);
+  }
+  SweepGraph<double> sweep64;
   for (int sweep = 0; sweep < kMaxSweeps && !converged; ++sweep) {
-    TNAD_CK(cudaMemsetAsync(flag, 0, sizeof(int), c->stream));
-    // Purely relative sweeps first: they drive null and noise-level columns to
-    // exact orthogonality (the triplets trg_svd's √s pullback relies on).  Only
-    // a spectrum that keeps re-rotating noise past kRelSweeps gets the floor.
-    const double ae = sweep < kRelSweeps ? 0.0 : abs_eps;
-    // pairs per round: NP/2 CTAs of 128 threads with the columns in registers
-    // (R rows per thread), or one warp per pair for very tall matrices
-    const unsigned np2 = (unsigned)(NP / 2);
+    // Purely relative sweeps first (rel_sweeps of them): they drive null and
+    // noise-level columns to exact orthogonality (the triplets trg_svd's √s
+    // pullback relies on).  Afterwards, or from the start for rel_sweeps = 0,
+    // the rounding floor applies: every triplet is then accurate to ε·‖A‖_F
+    // (the accuracy of LAPACK's SVD), and noise-level columns stop rotating.
+    const double ae = sweep < rel_sweeps ? 0.0 : abs_eps;
     // algorithmic FP64 work of one round: per pair 3 dot products (6m flops)
     // and one plane rotation of W (6m) and V (6n)
     const double round_flops = (double)(n / 2) * (12.0 * (double)m + 6.0 * (double)n);
-    for (int r = 0; r < NP - 1; ++r) {
-      KernelTimer kt(c, "jacobi_round", round_flops);
-      if (m <= 256)
-        k_jacobi_round_cta<2><<<np2, 128, 0, c->stream>>>(W, Vw, m, n, r, NP, tol, ae, fro2, flag);
-      else if (m <= 512)
-        k_jacobi_round_cta<4><<<np2, 128, 0, c->stream>>>(W, Vw, m, n, r, NP, tol, ae, fro2, flag);
-      else if (m <= 1024)
-        k_jacobi_round_cta<8><<<np2, 128, 0, c->stream>>>(W, Vw, m, n, r, NP, tol, ae, fro2, flag);
-      else if (m <= 2048)
-        k_jacobi_round_cta<16><<<np2, 128, 0, c->stream>>>(W, Vw, m, n, r, NP, tol, ae, fro2, flag);
-      else
+    if (m <= 2048) {
+      sweep64.run(c, "jacobi_round", W, Vw, m, n, NP, tol, ae, fro2, flag, round_flops);
+    } else {
+      TNAD_CK(cudaMemsetAsync(flag, 0, sizeof(int), c->stream));
+      for (int r = 0; r < NP - 1; ++r) {
+        KernelTimer kt(c, "jacobi_round", round_flops);
         k_jacobi_round<<<blocks, threads, 0, c->stream>>>(W, Vw, m, n, r, NP, tol, ae, fro2, flag);
+      }
+      count_launch(c, NP - 1);
+      check_launch(c, "jacobi_round");
     }
-    count_launch(c, NP - 1);
-    check_launch(c, "jacobi_round");
     TNAD_CK(cudaMemcpyAsync(c->h_flag, flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     TNAD_CK(cudaStreamSynchronize(c->stream));
     if (c->h_flag[0] == 0) converged = true;
@@ -509,7 +627,7 @@ extern "C" int tnad_svd_noalloc(const double* A, int m, int n, double* U, double
     if (cudaMemsetAsync(flag, 0, sizeof(int), st) != cudaSuccess) return TNAD_ERR_CUDA;
     const double ae = sweep < kRelSweeps ? 0.0 : abs_eps;
     for (int r = 0; r < NP - 1; ++r)
-      k_jacobi_round_cta<2><<<(unsigned)(NP / 2), 128, 0, st>>>(W, Vw, m, n, r, NP, tol, ae, fro2, flag);
+      k_jacobi_round_cta<2, double><<<(unsigned)(NP / 2), 128, 0, st>>>(W, Vw, m, n, r, NP, tol, ae, fro2, flag);
     if (cudaGetLastError() != cudaSuccess) return TNAD_ERR_CUDA;
     if (cudaMemcpyAsync(&hflag, flag, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)

@@ -199,8 +199,11 @@ Ten contract_shape(const Ten& A, const char* la, const Ten& B, const char* lb, c
 // ---------------- FP64 Jacobi SVD (jacobi.cu) ----------------
 // Thin SVD of m×n (m ≥ n) A: U m×n, S n (descending), V n×n.  A is not modified.
 // symmetric=true: A is symmetric, null-space columns of U are completed from V.
+// rel_sweeps: sweeps with the purely relative stop rule before the rounding
+// floor ε·‖A‖_F applies (relative accuracy of small triplets, needed where
+// √s of them is differentiated, as in TRG; 0 gives LAPACK-level accuracy).
 void svd_jacobi(tnad_ctx* c, const double* A, int64_t m, int64_t n, double* U, double* S,
-                double* V, bool symmetric);
+                double* V, bool symmetric, int rel_sweeps = 20);
 // Symmetric eigendecomposition of a small p×p matrix (p ≤ 256) by cyclic Jacobi in
 // one CTA: A = W·diag(lam)·Wᵀ, sorted by |lam| descending.
 void eigh_small(tnad_ctx* c, const double* A, int64_t p, double* W, double* lam);

@@ -153,9 +153,10 @@ def barrier(dist):
 # ---------------------------------------------------------------------------
 PEAKS_PATH = ROOT / "MEASURED_PEAKS.json"
 FP64_NOMINAL_TFLOPS = 1.25  # GB300 FP64 (no measured FP64 figure exists for this machine)
-# dram__bytes_read.sum + dram__bytes_write.sum per launch of the dominant kernel,
-# from the ncu capture summarised in profiles/jacobi_round_D4_chi64.md
-JACOBI_ROUND_TRAFFIC_BYTES = None
+# dram__bytes_read.sum + dram__bytes_write.sum per launch of the FP64 Jacobi round
+# (16 805 888 + 0 bytes; ncu flushes the caches between its passes), from the
+# capture summarised in profiles/jacobi_round_D4_chi64.md
+JACOBI_ROUND_TRAFFIC_BYTES = 16805888
 
 
 def peaks():

@@ -24,42 +24,47 @@ namespace tnad {
 // finite diagonal.  One CTA, right-looking, the matrix in shared memory.
 constexpr double kPivotFloor = 1e-14;
 
-__global__ void k_chol_factor(const double* __restrict__ G, int p, double* __restrict__ Rg, int* __restrict__ fail) {
+__global__ void __launch_bounds__(512) k_chol_factor(const double* __restrict__ G, int p, double* __restrict__ Rg,
+                                                     int* __restrict__ fail) {
   extern __shared__ double sm[];
-  const int ld = p + 1;  // padded: row accesses R[k, i..] hit distinct banks
-  double* R = sm;        // p × ld, column-major, upper triangle used
-  for (int e = threadIdx.x; e < p * p; e += blockDim.x) R[(e % p) + (e / p) * ld] = G[e];
-  __syncthreads();
+  const int ld = p + 1;  // padded leading dimension
+  double* A = sm;        // working copy of G (upper triangle), p × ld
+  __shared__ double piv[2];  // 1/d_k, sqrt(d_k) of the current step
   __shared__ int bad;
   __shared__ double floor_;
+  for (int e = threadIdx.x; e < p * p; e += blockDim.x) A[(e % p) + (e / p) * ld] = G[e];
+  __syncthreads();
   if (threadIdx.x == 0) {
     double mx = 0.0;
-    for (int k = 0; k < p; ++k) mx = fmax(mx, R[k + k * ld]);
+    for (int k = 0; k < p; ++k) mx = fmax(mx, A[k + k * ld]);
     bad = (mx > 0.0 && isfinite(mx)) ? 0 : 1;
     floor_ = bad ? 1e-300 : kPivotFloor * mx;
   }
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  // zeros below the diagonal of the output factor
+  for (int j = w; j < p; j += nw)
+    for (int i = j + 1 + lane; i < p; i += 32) Rg[i + (int64_t)j * p] = 0.0;
   __syncthreads();
-  // for k: R[k,k] = sqrt(R[k,k]); R[k,j] /= R[k,k] (j>k); trailing update
+  // right-looking, one barrier pair per pivot; warp w owns columns j ≡ w (mod nw)
+  // and its lanes the rows of each column:  R[k, j] = A[k, j]/√d_k and
+  // A[i, j] −= A[k, i]·A[k, j]/d_k for k < i ≤ j
   for (int k = 0; k < p; ++k) {
-    double d = R[k + k * ld];
-    if (!(d > floor_)) d = floor_;
-    const double rkk = sqrt(d);
-    __syncthreads();
-    if (threadIdx.x == 0) R[k + k * ld] = rkk;
-    const double inv = 1.0 / rkk;
-    for (int j = k + 1 + threadIdx.x; j < p; j += blockDim.x) R[k + j * ld] *= inv;
-    __syncthreads();
-    // trailing update of the upper triangle: R[i,j] -= R[k,i]·R[k,j] for k<i<=j
-    const int m = p - k - 1;
-    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
-      const int i = k + 1 + e % m, j = k + 1 + e / m;
-      if (i <= j) R[i + j * ld] -= R[k + i * ld] * R[k + j * ld];
+    if (threadIdx.x == 0) {
+      double d = A[k + k * ld];
+      if (!(d > floor_)) d = floor_;
+      piv[0] = 1.0 / d;
+      piv[1] = sqrt(d);
     }
     __syncthreads();
-  }
-  for (int e = threadIdx.x; e < p * p; e += blockDim.x) {
-    const int i = e % p, j = e / p;
-    Rg[e] = i <= j ? R[i + j * ld] : 0.0;
+    const double inv_d = piv[0], rkk = piv[1], inv_r = inv_d * rkk;  // 1/√d
+    for (int j = k + ((w - k) % nw + nw) % nw; j < p; j += nw) {
+      const double akj = A[k + j * ld];
+      if (lane == 0) Rg[k + (int64_t)j * p] = j == k ? rkk : akj * inv_r;
+      if (j == k) continue;
+      const double f = akj * inv_d;
+      for (int i = k + 1 + lane; i <= j; i += 32) A[i + j * ld] -= A[k + i * ld] * f;
+    }
+    __syncthreads();
   }
   if (threadIdx.x == 0 && bad) *fail = 1;
 }
@@ -103,7 +108,8 @@ void chol_inv_upper(tnad_ctx* c, const double* G, int64_t p, double* Rinv, int* 
   }
   WsScope scope(c);
   double* R = ws_d(c, p * p);
-  k_chol_factor<<<1, 256, (size_t)p * (p + 1) * 8, c->stream>>>(G, (int)p, R, dev_fail);
+  KernelTimer kt(c, "chol", (double)p * p * p / 3.0);
+  k_chol_factor<<<1, 512, (size_t)p * (p + 1) * 8, c->stream>>>(G, (int)p, R, dev_fail);
   k_tri_inv<<<(unsigned)((p + 7) / 8), 256, (size_t)(p * (p + 1) + 9 * p) * 8, c->stream>>>(R, (int)p, Rinv);
   count_launch(c, 2);
   check_launch(c, "chol_inv");
@@ -169,8 +175,9 @@ __global__ void k_eigh_jacobi(const double* __restrict__ A, int p, int max_sweep
             b = t;
           }
           const T apq = H[a + b * ld], app = H[a + a * ld], aqq = H[b + b * ld];
-          if (apq != (T)0 && fabs((double)apq) > (double)tol * sqrt(fabs((double)app * (double)aqq)) &&
-              fabs((double)apq) > (double)absfl && fabs((double)apq) > 1e-300) {
+          // stop rule in the kernel's own precision (an FP64 test in the FP32
+          // kernel would run on GB300's narrow FP64 pipe)
+          if (apq != (T)0 && fabs(apq) > tol * sqrt(fabs(app)) * sqrt(fabs(aqq)) && fabs(apq) > absfl) {
             const T tau = (aqq - app) / ((T)2 * apq);
             const T t = (tau >= (T)0 ? (T)1 : (T)-1) / (fabs(tau) + sqrt((T)1 + tau * tau));
             c = (T)1 / sqrt((T)1 + t * t);
@@ -247,6 +254,7 @@ void eigh_small_prec(tnad_ctx* c, bool fp32, const double* A, int64_t p, double*
   TNAD_REQUIRE(sm <= kMaxSm, TNAD_ERR_SHAPE, "eigh_small: matrix does not fit in shared memory");
   static std::atomic<bool> attr32{false}, attr64{false};
   // eigenvectors accumulate in global memory (L1-cached); H lives in shared memory
+  KernelTimer kt(c, fp32 ? "eigh_f32" : "eigh_f64", 0.0);
   if (fp32) {
     if (!attr32) {
       TNAD_CK(cudaFuncSetAttribute(k_eigh_jacobi<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSm));
@@ -343,6 +351,7 @@ void polar_ns(tnad_ctx* c, const double* X, int64_t m, int iters, double* O, int
     TNAD_CK(cudaFuncSetAttribute(k_polar_ns, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 129 * 128 * 4));
     attr = true;
   }
+  KernelTimer kt(c, "polar_ns", 0.0);
   k_polar_ns<<<1, 1024, (size_t)2 * (m + 1) * m * 4, c->stream>>>(X, (int)m, iters, O, dev_info);
   count_launch(c);
   check_launch(c, "polar_ns");

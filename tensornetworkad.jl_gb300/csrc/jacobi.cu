@@ -145,20 +145,25 @@ __global__ void __launch_bounds__(128) k_jacobi_round_cta(T* __restrict__ W, T* 
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    const double A = (double)red[0][0] + red[0][1] + red[0][2] + red[0][3];
-    const double B = (double)red[1][0] + red[1][1] + red[1][2] + red[1][3];
-    const double G = (double)red[2][0] + red[2][1] + red[2][2] + red[2][3];
-    double cs = 1.0, sn = 0.0;
-    if (G != 0.0 && A != 0.0 && B != 0.0 &&
-        fabs(G) > tol * sqrt(A) * sqrt(B) + abs_eps * sqrt(fro2[0]) * (sqrt(A) + sqrt(B))) {
-      const double zeta = (B - A) / (2.0 * G);
-      const double t = fabs(zeta) > 1e150 ? 0.5 / zeta : copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-      cs = 1.0 / sqrt(1.0 + t * t);
+    // The stop test and the rotation angle are formed in the sweep's own
+    // precision: on GB300 the FP64 square roots and divisions of this single
+    // thread sit on the round's critical path.
+    const T A = red[0][0] + red[0][1] + red[0][2] + red[0][3];
+    const T B = red[1][0] + red[1][1] + red[1][2] + red[1][3];
+    const T G = red[2][0] + red[2][1] + red[2][2] + red[2][3];
+    T cs = 1, sn = 0;
+    const T sa = sqrt(A), sb = sqrt(B);
+    if (G != (T)0 && A != (T)0 && B != (T)0 &&
+        fabs(G) > (T)tol * sa * sb + (T)abs_eps * sqrt((T)fro2[0]) * (sa + sb)) {
+      const T zeta = (B - A) / ((T)2 * G);
+      const T big = sizeof(T) == 8 ? (T)1e150 : (T)1e18;
+      const T t = fabs(zeta) > big ? (T)0.5 / zeta : copysign((T)1, zeta) / (fabs(zeta) + sqrt((T)1 + zeta * zeta));
+      cs = (T)1 / sqrt((T)1 + t * t);
       sn = cs * t;
       atomicAdd(rotated, 1);
     }
-    rot[0] = (T)cs;
-    rot[1] = (T)sn;
+    rot[0] = cs;
+    rot[1] = sn;
   }
   __syncthreads();
   const T cs = rot[0], sn = rot[1];
@@ -458,7 +463,7 @@ void svd_jacobi(tnad_ctx* c, const double* A, int64_t m, int64_t n, double* U, d
       sweep32.run(c, "jacobi_round_f32", W32, V32, m, n, NP, tol32, ae32, fro2, flag, round_flops);
       TNAD_CK(cudaMemcpyAsync(c->h_flag, flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
       TNAD_CK(cudaStreamSynchronize(c->stream));
-      if (c->h_flag[0] <= (int)(n / 64)) break;  // a few stragglers are left to FP64
+      if (c->h_flag[0] <= 2) break;  // converged at FP32 accuracy (a straggler or two is left to FP64)
     }
     k_to_double<<<(int)nb_nn, 256, 0, c->stream>>>(V32, n * n, Vw);
     count_launch(c);

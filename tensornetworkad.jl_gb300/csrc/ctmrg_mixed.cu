@@ -139,7 +139,9 @@ void align_polar(tnad_ctx* c, int prec, double* z, const double* zprev, int64_t 
 // Y (n×p) → Q (n×p) with orthonormal columns spanning the same nested leading
 // subspaces: two CholeskyQR passes (Gram in FP64).  A tiny random component
 // (relative `jitter`) keeps Y full rank when M has fewer than p non-null
-// directions (the zero-padded raw environment of the first steps).
+// directions (the zero-padded raw environment of the first steps).  The
+// factorisation stays in FP64: CholeskyQR in FP32 (even shifted, as in
+// CholeskyQR3) breaks down on these nearly rank-deficient blocks.
 void cholqr2(tnad_ctx* c, int prec, const double* Y, int64_t n, int64_t p, double* Q, double jitter, uint64_t seed) {
   WsScope scope(c);
   double* G = ws_d(c, p * p);
@@ -162,6 +164,32 @@ void cholqr2(tnad_ctx* c, int prec, const double* Y, int64_t n, int64_t p, doubl
       src = t;
     }
   }
+}
+
+// FP64 eigendecomposition of the p×p Rayleigh–Ritz matrix H: the FP32 Jacobi
+// solver first, its eigenvectors re-orthogonalised in FP64 (Newton–Schulz),
+// then FP64 Jacobi on the nearly diagonal H' = WᵀHW (two or three sweeps
+// instead of ~10 from scratch on GB300's narrow FP64 pipe), W ← W·W'.
+void eigh_small_refined(tnad_ctx* c, const double* H, int64_t p, double* W, double* lam, int* dev_info) {
+  WsScope scope(c);
+  double* W0 = ws_d(c, p * p);
+  double* G = ws_d(c, p * p);
+  double* T1 = ws_d(c, p * p);
+  double* Hp = ws_d(c, p * p);
+  double* Wp = ws_d(c, p * p);
+  eigh_small_prec(c, true, H, p, W0, lam, 40, dev_info);
+  for (int it = 0; it < 2; ++it) {
+    gemm_f64(c, 'T', 'N', p, p, p, 1.0, W0, p, W0, p, 0.0, G, p);
+    copy_d2d(c, T1, W0, p * p);
+    gemm_f64(c, 'N', 'N', p, p, p, -0.5, W0, p, G, p, 1.5, T1, p);
+    copy_d2d(c, W0, T1, p * p);
+  }
+  gemm_f64(c, 'N', 'N', p, p, p, 1.0, H, p, W0, p, 0.0, T1, p);
+  gemm_f64(c, 'T', 'N', p, p, p, 1.0, W0, p, T1, p, 0.0, Hp, p);
+  k_symmetrize_small<<<nb(p * p), 256, 0, c->stream>>>(Hp, (int)p);
+  count_launch(c);
+  eigh_small_prec(c, false, Hp, p, Wp, lam, 40, dev_info);
+  gemm_f64(c, 'N', 'N', p, p, p, 1.0, W0, p, Wp, p, 0.0, W, p);
 }
 
 MixedRun ctmrg_run_mixed(tnad_ctx* c, const double* a_, int d, int chi, double* C, double* T, double tol, int maxit,
@@ -219,16 +247,25 @@ MixedRun ctmrg_run_mixed(tnad_ctx* c, const double* a_, int d, int chi, double* 
     // zero-padded early environments have fewer than p non-null directions; at
     // the FP64 polishing stage it is below the rounding of the result.
     const double jitter = (dprev > 1e-3 || prec != TNAD_PREC_FP64) ? 1e-7 : 1e-13;
+    // the block is re-orthonormalised every second power step: two products
+    // raise κ by at most (|λ₁|/|λ_p|)², far inside what FP64 CholeskyQR2 takes
     for (int it = 0; it < inner; ++it) {
       gemm(c, prec, 'N', 'N', n, p, n, 1.0, M, n, Q, n, 0.0, Y, n);
-      if (it + 1 < inner) cholqr2(c, prec, Y, n, p, Q, jitter, 1000 + it);
+      if (it + 1 == inner) break;
+      if ((inner - 1 - it) % 2 == 1)
+        cholqr2(c, prec, Y, n, p, Q, jitter, 1000 + it);
+      else
+        copy_d2d(c, Q, Y, n * p);
     }
     // Rayleigh–Ritz in span(Q)
     tr.mark(prec == TNAD_PREC_FP64 ? "ritz_f64" : "ritz_tf32");
     gemm_f64(c, 'T', 'N', p, p, n, 1.0, Q, n, Y, n, 0.0, H, p);
     k_symmetrize_small<<<nb(p * p), 256, 0, c->stream>>>(H, (int)p);
     count_launch(c);
-    eigh_small_prec(c, prec != TNAD_PREC_FP64, H, p, Wm, lam, 40, c->d_flag + 17);
+    if (prec == TNAD_PREC_FP64)
+      eigh_small_refined(c, H, p, Wm, lam, c->d_flag + 17);
+    else
+      eigh_small_prec(c, true, H, p, Wm, lam, 40, c->d_flag + 17);
     gemm(c, prec, 'N', 'N', n, chi, p, 1.0, Q, n, Wm, p, 0.0, z, n);
     // Gauge: rotate the Ritz basis onto the previous projector (orthogonal
     // Procrustes, z ← z·polar(zᵀ·z_prev)).  Consecutive environments then agree

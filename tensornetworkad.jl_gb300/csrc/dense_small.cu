@@ -24,21 +24,22 @@ namespace tnad {
 // finite diagonal.  One CTA, right-looking, the matrix in shared memory.
 constexpr double kPivotFloor = 1e-14;
 
-__global__ void __launch_bounds__(512) k_chol_factor(const double* __restrict__ G, int p, double* __restrict__ Rg,
-                                                     int* __restrict__ fail) {
-  extern __shared__ double sm[];
-  const int ld = p + 1;  // padded leading dimension
-  double* A = sm;        // working copy of G (upper triangle), p × ld
-  __shared__ double piv[2];  // 1/d_k, sqrt(d_k) of the current step
+template <typename T>
+__global__ void __launch_bounds__(512) k_chol_factor(const double* __restrict__ G, int p, double floor_rel,
+                                                     double* __restrict__ Rg, int* __restrict__ fail) {
+  extern __shared__ unsigned char sm_raw[];
+  T* A = reinterpret_cast<T*>(sm_raw);  // working copy of G (upper triangle), p × ld
+  const int ld = p + 1;                 // padded leading dimension
+  __shared__ T piv[2];                  // 1/d_k, sqrt(d_k) of the current step
   __shared__ int bad;
-  __shared__ double floor_;
-  for (int e = threadIdx.x; e < p * p; e += blockDim.x) A[(e % p) + (e / p) * ld] = G[e];
+  __shared__ T floor_;
+  for (int e = threadIdx.x; e < p * p; e += blockDim.x) A[(e % p) + (e / p) * ld] = (T)G[e];
   __syncthreads();
   if (threadIdx.x == 0) {
-    double mx = 0.0;
+    T mx = 0;
     for (int k = 0; k < p; ++k) mx = fmax(mx, A[k + k * ld]);
-    bad = (mx > 0.0 && isfinite(mx)) ? 0 : 1;
-    floor_ = bad ? 1e-300 : kPivotFloor * mx;
+    bad = (mx > (T)0 && isfinite(mx)) ? 0 : 1;
+    floor_ = bad ? (T)1e-30 : (T)floor_rel * mx;
   }
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   // zeros below the diagonal of the output factor
@@ -50,18 +51,18 @@ __global__ void __launch_bounds__(512) k_chol_factor(const double* __restrict__ 
   // A[i, j] −= A[k, i]·A[k, j]/d_k for k < i ≤ j
   for (int k = 0; k < p; ++k) {
     if (threadIdx.x == 0) {
-      double d = A[k + k * ld];
+      T d = A[k + k * ld];
       if (!(d > floor_)) d = floor_;
-      piv[0] = 1.0 / d;
+      piv[0] = (T)1 / d;
       piv[1] = sqrt(d);
     }
     __syncthreads();
-    const double inv_d = piv[0], rkk = piv[1], inv_r = inv_d * rkk;  // 1/√d
+    const T inv_d = piv[0], rkk = piv[1], inv_r = inv_d * rkk;  // 1/√d
     for (int j = k + ((w - k) % nw + nw) % nw; j < p; j += nw) {
-      const double akj = A[k + j * ld];
-      if (lane == 0) Rg[k + (int64_t)j * p] = j == k ? rkk : akj * inv_r;
+      const T akj = A[k + j * ld];
+      if (lane == 0) Rg[k + (int64_t)j * p] = (double)(j == k ? rkk : akj * inv_r);
       if (j == k) continue;
-      const double f = akj * inv_d;
+      const T f = akj * inv_d;
       for (int i = k + 1 + lane; i <= j; i += 32) A[i + j * ld] -= A[k + i * ld] * f;
     }
     __syncthreads();
@@ -72,47 +73,55 @@ __global__ void __launch_bounds__(512) k_chol_factor(const double* __restrict__ 
 // Rinv = R⁻¹ for upper-triangular R (p×p): one warp per column j solves
 // R·x = e_j by back substitution (lanes split each row's dot product), R in
 // shared memory with leading dimension p+1; 8 columns per CTA.
+template <typename T>
 __global__ void k_tri_inv(const double* __restrict__ Rg, int p, double* __restrict__ Rinv) {
-  extern __shared__ double sm[];
+  extern __shared__ unsigned char sm_raw[];
+  T* R = reinterpret_cast<T*>(sm_raw);  // p × ld
   const int ld = p + 1;
-  double* R = sm;              // p × ld
-  double* rd = sm + p * ld;    // 1/R[i,i]
-  double* X = rd + p;          // 8 × p solution columns
+  T* rd = R + p * ld;  // 1/R[i,i]
+  T* X = rd + p;       // 8 × p solution columns
   for (int e = threadIdx.x; e < p * p; e += blockDim.x) {
     const int i = e % p, j = e / p;
-    R[i + j * ld] = Rg[e];
+    R[i + j * ld] = (T)Rg[e];
   }
-  for (int i = threadIdx.x; i < p; i += blockDim.x) rd[i] = 1.0 / Rg[i + (int64_t)i * p];
+  for (int i = threadIdx.x; i < p; i += blockDim.x) rd[i] = (T)1 / (T)Rg[i + (int64_t)i * p];
   __syncthreads();
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int j = blockIdx.x * 8 + w;
   if (j >= p) return;
-  double* x = X + w * p;
+  T* x = X + w * p;
   for (int i = j; i >= 0; --i) {
-    double s = 0.0;
+    T s = 0;
     for (int l = i + 1 + lane; l <= j; l += 32) s += R[i + l * ld] * x[l];
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) x[i] = ((i == j ? 1.0 : 0.0) - s) * rd[i];
+    if (lane == 0) x[i] = ((i == j ? (T)1 : (T)0) - s) * rd[i];
     __syncwarp();
   }
-  for (int i = lane; i < p; i += 32) Rinv[i + (int64_t)j * p] = i <= j ? x[i] : 0.0;
+  for (int i = lane; i < p; i += 32) Rinv[i + (int64_t)j * p] = i <= j ? (double)x[i] : 0.0;
 }
 
-void chol_inv_upper(tnad_ctx* c, const double* G, int64_t p, double* Rinv, int* dev_fail) {
-  TNAD_REQUIRE(p >= 1 && p <= 160, TNAD_ERR_SHAPE, "chol_inv_upper: p must be in [1,160]");
+template <typename T>
+void chol_inv_t(tnad_ctx* c, const double* G, int64_t p, double floor_rel, double* Rinv, int* dev_fail) {
   static std::atomic<bool> attr{false};
+  const size_t es = sizeof(T);
   if (!attr) {
-    TNAD_CK(cudaFuncSetAttribute(k_chol_factor, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 161 * 8));
-    TNAD_CK(cudaFuncSetAttribute(k_tri_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (160 * 161 + 9 * 160) * 8));
+    TNAD_CK(cudaFuncSetAttribute(k_chol_factor<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(160 * 161 * es)));
+    TNAD_CK(cudaFuncSetAttribute(k_tri_inv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)((160 * 161 + 9 * 160) * es)));
     attr = true;
   }
   WsScope scope(c);
   double* R = ws_d(c, p * p);
   KernelTimer kt(c, "chol", (double)p * p * p / 3.0);
-  k_chol_factor<<<1, 512, (size_t)p * (p + 1) * 8, c->stream>>>(G, (int)p, R, dev_fail);
-  k_tri_inv<<<(unsigned)((p + 7) / 8), 256, (size_t)(p * (p + 1) + 9 * p) * 8, c->stream>>>(R, (int)p, Rinv);
+  k_chol_factor<T><<<1, 512, (size_t)p * (p + 1) * es, c->stream>>>(G, (int)p, floor_rel, R, dev_fail);
+  k_tri_inv<T><<<(unsigned)((p + 7) / 8), 256, (size_t)(p * (p + 1) + 9 * p) * es, c->stream>>>(R, (int)p, Rinv);
   count_launch(c, 2);
   check_launch(c, "chol_inv");
+}
+
+void chol_inv_upper(tnad_ctx* c, const double* G, int64_t p, double* Rinv, int* dev_fail) {
+  TNAD_REQUIRE(p >= 1 && p <= 160, TNAD_ERR_SHAPE, "chol_inv_upper: p must be in [1,160]");
+  chol_inv_t<double>(c, G, p, kPivotFloor, Rinv, dev_fail);
 }
 
 // ---------------------------------------------------------------- Jacobi eigh

@@ -296,8 +296,10 @@ __global__ void k_polar_ns(const double* __restrict__ X, int m, int iters, doubl
   extern __shared__ float psm[];
   const int ld = m + 1;         // padded leading dimension (bank-conflict free)
   float* A = psm;               // m×m current iterate
-  float* G = psm + m * ld;      // m×m scratch
+  float* G = psm + m * ld;      // AᵀA
+  float* B = psm + 2 * m * ld;  // next iterate
   __shared__ float red[32];
+  __shared__ int done;
   const int mm = m * m;
   // scale by 1/‖X‖_F·√m so that all singular values are ≤ 1 < √3
   float s = 0.f;
@@ -314,54 +316,58 @@ __global__ void k_polar_ns(const double* __restrict__ X, int m, int iters, doubl
   const float sc = fminf(red[0], 1.0f) * 0.999f;
   for (int e = threadIdx.x; e < mm; e += blockDim.x) A[(e % m) + (e / m) * ld] = (float)X[e] * (red[0] > 1.f ? sc : 1.0f);
   __syncthreads();
-  for (int it = 0; it < iters; ++it) {
-    // G = AᵀA
+  float worst = 0.f;
+  for (int it = 0; it <= iters; ++it) {
+    // G = AᵀA, and how far it is from I
+    float dev = 0.f;
     for (int e = threadIdx.x; e < mm; e += blockDim.x) {
       const int i = e % m, j = e / m;
       float acc = 0.f;
       for (int k = 0; k < m; ++k) acc += A[k + i * ld] * A[k + j * ld];
       G[i + j * ld] = acc;
+      dev = fmaxf(dev, fabsf(acc - (i == j ? 1.f : 0.f)));
+    }
+    for (int o = 16; o > 0; o >>= 1) dev = fmaxf(dev, __shfl_xor_sync(0xffffffffu, dev, o));
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = dev;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float t = 0.f;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t = fmaxf(t, red[w]);
+      red[0] = t;
+      // all iterations run: the FP32 iterate must reach the polar factor to FP32
+      // accuracy (stopping at an orthogonality of 1e-5 and polishing in FP64
+      // gave a visibly worse-conditioned fixed-point adjoint)
+      done = it == iters ? 1 : 0;
     }
     __syncthreads();
-    // A ← A·(1.5 I − 0.5 G)   (row i of A times G; one thread per element, into O as scratch)
+    worst = red[0];
+    if (done) break;
+    // B = A·(1.5 I − 0.5 G)
     for (int e = threadIdx.x; e < mm; e += blockDim.x) {
       const int i = e % m, j = e / m;
       float acc = 1.5f * A[i + j * ld];
       for (int k = 0; k < m; ++k) acc -= 0.5f * A[i + k * ld] * G[k + j * ld];
-      O[e] = (double)acc;
+      B[i + j * ld] = acc;
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < mm; e += blockDim.x) A[(e % m) + (e / m) * ld] = (float)O[e];
-    __syncthreads();
+    float* t = A;
+    A = B;
+    B = t;
   }
-  // orthogonality check
-  float worst = 0.f;
-  for (int e = threadIdx.x; e < mm; e += blockDim.x) {
-    const int i = e % m, j = e / m;
-    float acc = 0.f;
-    for (int k = 0; k < m; ++k) acc += A[k + i * ld] * A[k + j * ld];
-    worst = fmaxf(worst, fabsf(acc - (i == j ? 1.f : 0.f)));
-  }
-  for (int o = 16; o > 0; o >>= 1) worst = fmaxf(worst, __shfl_xor_sync(0xffffffffu, worst, o));
-  __syncthreads();
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = worst;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    float t = 0.f;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t = fmaxf(t, red[w]);
-    info[0] = t < 1e-4f ? 1 : 0;
-  }
+  for (int e = threadIdx.x; e < mm; e += blockDim.x) O[e] = (double)A[(e % m) + (e / m) * ld];
+  if (threadIdx.x == 0) info[0] = worst < 1e-4f ? 1 : 0;
 }
 
 void polar_ns(tnad_ctx* c, const double* X, int64_t m, int iters, double* O, int* dev_info) {
   TNAD_REQUIRE(m >= 1 && m <= 128, TNAD_ERR_SHAPE, "polar_ns: m must be in [1,128]");
   static std::atomic<bool> attr{false};
   if (!attr) {
-    TNAD_CK(cudaFuncSetAttribute(k_polar_ns, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * 129 * 128 * 4));
+    TNAD_CK(cudaFuncSetAttribute(k_polar_ns, cudaFuncAttributeMaxDynamicSharedMemorySize, 3 * 129 * 128 * 4));
     attr = true;
   }
   KernelTimer kt(c, "polar_ns", 0.0);
-  k_polar_ns<<<1, 1024, (size_t)2 * (m + 1) * m * 4, c->stream>>>(X, (int)m, iters, O, dev_info);
+  k_polar_ns<<<1, 1024, (size_t)3 * (m + 1) * m * 4, c->stream>>>(X, (int)m, iters, O, dev_info);
   count_launch(c);
   check_launch(c, "polar_ns");
 }

@@ -10,6 +10,8 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <mutex>
 
 #include "tnad_internal.h"
@@ -442,6 +444,7 @@ void svd_jacobi(tnad_ctx* c, const double* A, int64_t m, int64_t n, double* U, d
   const double weak_rel = 1e-8;
   int* flag = c->d_flag;
   bool converged = (n == 1);
+  const bool trace = std::getenv("TNAD_TRACE") != nullptr;  // per-sweep rotation counts to stderr
   const int threads = 256;
   const int blocks = (NP / 2 * 32 + threads - 1) / threads;
   const int64_t nb_nn = std::min<int64_t>((n * n + 255) / 256, 4096);
@@ -463,6 +466,7 @@ void svd_jacobi(tnad_ctx* c, const double* A, int64_t m, int64_t n, double* U, d
       sweep32.run(c, "jacobi_round_f32", W32, V32, m, n, NP, tol32, ae32, fro2, flag, round_flops);
       TNAD_CK(cudaMemcpyAsync(c->h_flag, flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
       TNAD_CK(cudaStreamSynchronize(c->stream));
+      if (trace) std::fprintf(stderr, "[tnad trace] svd n=%lld fp32 sweep %d rotations %d\n", (long long)n, sweep, c->h_flag[0]);
       if (c->h_flag[0] <= 2) break;  // converged at FP32 accuracy (a straggler or two is left to FP64)
     }
     k_to_double<<<(int)nb_nn, 256, 0, c->stream>>>(V32, n * n, Vw);
@@ -502,6 +506,7 @@ void svd_jacobi(tnad_ctx* c, const double* A, int64_t m, int64_t n, double* U, d
     }
     TNAD_CK(cudaMemcpyAsync(c->h_flag, flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     TNAD_CK(cudaStreamSynchronize(c->stream));
+    if (trace) std::fprintf(stderr, "[tnad trace] svd n=%lld fp64 sweep %d rotations %d\n", (long long)n, sweep, c->h_flag[0]);
     if (c->h_flag[0] == 0) converged = true;
   }
   TNAD_REQUIRE(converged, TNAD_ERR_NOT_CONVERGED, "svd_jacobi: no convergence within the sweep cap");

@@ -14,6 +14,7 @@
 // the reference's; z columns are sign-aligned with the previous step's so that
 // the converged environment is a strict fixed point (used by the implicit adjoint).
 #include <cmath>
+#include <cstdio>
 #include <limits>
 
 #include "tnad_mixed.h"
@@ -21,6 +22,7 @@
 namespace tnad {
 
 void chol_inv_upper(tnad_ctx* c, const double* G, int64_t p, double* Rinv, int* dev_fail);
+void chol_inv_upper_f32(tnad_ctx* c, const double* G, int64_t p, double* Rinv, int* dev_fail);
 void eigh_small_prec(tnad_ctx* c, bool fp32, const double* A, int64_t p, double* W, double* lam, int max_sweeps,
                      int* dev_info);
 void randn(tnad_ctx* c, double* x, int64_t n, uint64_t seed, double scale, bool accumulate,
@@ -140,7 +142,7 @@ void align_polar(tnad_ctx* c, int prec, double* z, const double* zprev, int64_t 
 // subspaces: two CholeskyQR passes (Gram in FP64).  A tiny random component
 // (relative `jitter`) keeps Y full rank when M has fewer than p non-null
 // directions (the zero-padded raw environment of the first steps).  The
-// factorisation stays in FP64: CholeskyQR in FP32 (even shifted, as in
+// first factorisation stays in FP64: CholeskyQR in FP32 (even shifted, as in
 // CholeskyQR3) breaks down on these nearly rank-deficient blocks.
 void cholqr2(tnad_ctx* c, int prec, const double* Y, int64_t n, int64_t p, double* Q, double jitter, uint64_t seed) {
   WsScope scope(c);
@@ -157,7 +159,12 @@ void cholqr2(tnad_ctx* c, int prec, const double* Y, int64_t n, int64_t p, doubl
   const double* src = t;
   for (int pass = 0; pass < 2; ++pass) {
     gemm_f64(c, 'T', 'N', p, p, n, 1.0, src, n, src, n, 0.0, G, p);
-    chol_inv_upper(c, G, p, Ri, fail);
+    // the second Gram matrix is I + O(κ(Y)²·ε64): at TF32X3 accuracy its
+    // factor is taken in FP32 (GB300's FP32 pipe is far wider than its FP64 one)
+    if (pass == 1 && prec != TNAD_PREC_FP64)
+      chol_inv_upper_f32(c, G, p, Ri, fail);
+    else
+      chol_inv_upper(c, G, p, Ri, fail);
     gemm(c, prec, 'N', 'N', n, p, p, 1.0, src, n, Ri, p, 0.0, Q, n);
     if (pass == 0) {
       copy_d2d(c, t, Q, n * p);
@@ -266,6 +273,11 @@ MixedRun ctmrg_run_mixed(tnad_ctx* c, const double* a_, int d, int chi, double* 
       eigh_small_refined(c, H, p, Wm, lam, c->d_flag + 17);
     else
       eigh_small_prec(c, true, H, p, Wm, lam, 40, c->d_flag + 17);
+    if (tr.on()) {
+      TNAD_CK(cudaMemcpyAsync(c->h_flag + 17, c->d_flag + 17, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+      TNAD_CK(cudaStreamSynchronize(c->stream));
+      std::fprintf(stderr, "[tnad trace] step %d ritz eigh sweeps %d (inner %d)\n", k, c->h_flag[17], inner);
+    }
     gemm(c, prec, 'N', 'N', n, chi, p, 1.0, Q, n, Wm, p, 0.0, z, n);
     // Gauge: rotate the Ritz basis onto the previous projector (orthogonal
     // Procrustes, z ← z·polar(zᵀ·z_prev)).  Consecutive environments then agree

@@ -124,6 +124,14 @@ void chol_inv_upper(tnad_ctx* c, const double* G, int64_t p, double* Rinv, int* 
   chol_inv_t<double>(c, G, p, kPivotFloor, Rinv, dev_fail);
 }
 
+// FP32 factorisation (relative pivot floor 1e-7) for Gram matrices that are
+// already close to I: the second CholeskyQR pass while the contractions run
+// at TF32X3 accuracy.
+void chol_inv_upper_f32(tnad_ctx* c, const double* G, int64_t p, double* Rinv, int* dev_fail) {
+  TNAD_REQUIRE(p >= 1 && p <= 160, TNAD_ERR_SHAPE, "chol_inv_upper_f32: p must be in [1,160]");
+  chol_inv_t<float>(c, G, p, 1e-7, Rinv, dev_fail);
+}
+
 // ---------------------------------------------------------------- Jacobi eigh
 __device__ __forceinline__ void circle_pair(int r, int k, int NP, int* p, int* q) {
   if (k == 0) {

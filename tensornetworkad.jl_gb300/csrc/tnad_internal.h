@@ -104,6 +104,7 @@ class PhaseTrace {
   PhaseTrace(tnad_ctx* c, const char* name);
   ~PhaseTrace();
   void mark(const char* phase);  // closes the previous phase, opens `phase`
+  bool on() const { return on_; }
 
  private:
   tnad_ctx* c_;

@@ -210,34 +210,36 @@ __global__ void k_eigh_jacobi(const double* __restrict__ A, int p, int max_sweep
         sn_[k] = s;
       }
       __syncthreads();
+      // warp w takes pairs k ≡ w (mod warps), its lanes the matrix index (no
+      // integer division in the inner loops)
+      const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
       // rows: (row a, row b) ← (c·row a − s·row b, s·row a + c·row b)
-      for (int e = threadIdx.x; e < (NP / 2) * p; e += blockDim.x) {
-        const int k = e / p, col = e % p;
+      for (int k = wid; k < NP / 2; k += nwarp) {
         const int a = pp_[k], b = qq_[k];
         if (a < 0 || sn_[k] == (T)0) continue;
         const T c = cs_[k], s = sn_[k];
-        const T x = H[a + col * ld], y = H[b + col * ld];
-        H[a + col * ld] = c * x - s * y;
-        H[b + col * ld] = s * x + c * y;
+        for (int col = lane; col < p; col += 32) {
+          const T x = H[a + col * ld], y = H[b + col * ld];
+          H[a + col * ld] = c * x - s * y;
+          H[b + col * ld] = s * x + c * y;
+        }
       }
       __syncthreads();
-      // columns of H and of Z
-      for (int e = threadIdx.x; e < (NP / 2) * p; e += blockDim.x) {
-        const int k = e / p, row = e % p;
+      // columns of H and of Z; then the rotated pair's off-diagonal entry is 0
+      for (int k = wid; k < NP / 2; k += nwarp) {
         const int a = pp_[k], b = qq_[k];
         if (a < 0 || sn_[k] == (T)0) continue;
         const T c = cs_[k], s = sn_[k];
-        const T x = H[row + a * ld], y = H[row + b * ld];
-        H[row + a * ld] = c * x - s * y;
-        H[row + b * ld] = s * x + c * y;
-        const T zx = Z[row + a * p], zy = Z[row + b * p];
-        Z[row + a * p] = c * zx - s * zy;
-        Z[row + b * p] = s * zx + c * zy;
-      }
-      __syncthreads();
-      for (int k = threadIdx.x; k < NP / 2; k += blockDim.x) {
-        const int a = pp_[k], b = qq_[k];
-        if (a >= 0 && sn_[k] != (T)0) {
+        for (int row = lane; row < p; row += 32) {
+          const T x = H[row + a * ld], y = H[row + b * ld];
+          H[row + a * ld] = c * x - s * y;
+          H[row + b * ld] = s * x + c * y;
+          const T zx = Z[row + a * p], zy = Z[row + b * p];
+          Z[row + a * p] = c * zx - s * zy;
+          Z[row + b * p] = s * zx + c * zy;
+        }
+        __syncwarp();
+        if (lane == 0) {
           H[a + b * ld] = (T)0;
           H[b + a * ld] = (T)0;
         }

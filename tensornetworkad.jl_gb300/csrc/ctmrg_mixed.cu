@@ -173,17 +173,32 @@ void cholqr2(tnad_ctx* c, int prec, const double* Y, int64_t n, int64_t p, doubl
   }
 }
 
+// λ_i = S_i·sign(U_i·V_i): eigenvalues of a symmetric matrix from its SVD
+// (one warp per column)
+__global__ void k_eig_from_svd(const double* __restrict__ U, const double* __restrict__ V,
+                               const double* __restrict__ S, int p, double* __restrict__ lam) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= p) return;
+  double d = 0.0;
+  for (int i = lane; i < p; i += 32) d += U[i + (int64_t)w * p] * V[i + (int64_t)w * p];
+  for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+  if (lane == 0) lam[w] = d < 0.0 ? -S[w] : S[w];
+}
+
 // FP64 eigendecomposition of the p×p Rayleigh–Ritz matrix H: the FP32 Jacobi
 // solver first, its eigenvectors re-orthogonalised in FP64 (Newton–Schulz),
-// then FP64 Jacobi on the nearly diagonal H' = WᵀHW (two or three sweeps
-// instead of ~10 from scratch on GB300's narrow FP64 pipe), W ← W·W'.
+// then the nearly diagonal H' = WᵀHW finished by the multi-CTA FP64 Jacobi
+// SVD (one CTA per column pair, sweeps replayed as CUDA graphs: GB300's FP64
+// pipe is too narrow for a one-SM FP64 solver), W ← W·V'.
 void eigh_small_refined(tnad_ctx* c, const double* H, int64_t p, double* W, double* lam, int* dev_info) {
   WsScope scope(c);
   double* W0 = ws_d(c, p * p);
   double* G = ws_d(c, p * p);
   double* T1 = ws_d(c, p * p);
   double* Hp = ws_d(c, p * p);
-  double* Wp = ws_d(c, p * p);
+  double* Up = ws_d(c, p * p);
+  double* Sp = ws_d(c, p);
+  double* Vp = ws_d(c, p * p);
   eigh_small_prec(c, true, H, p, W0, lam, 40, dev_info);
   for (int it = 0; it < 2; ++it) {
     gemm_f64(c, 'T', 'N', p, p, p, 1.0, W0, p, W0, p, 0.0, G, p);
@@ -195,8 +210,10 @@ void eigh_small_refined(tnad_ctx* c, const double* H, int64_t p, double* W, doub
   gemm_f64(c, 'T', 'N', p, p, p, 1.0, W0, p, T1, p, 0.0, Hp, p);
   k_symmetrize_small<<<nb(p * p), 256, 0, c->stream>>>(Hp, (int)p);
   count_launch(c);
-  eigh_small_prec(c, false, Hp, p, Wp, lam, 40, dev_info);
-  gemm_f64(c, 'N', 'N', p, p, p, 1.0, W0, p, Wp, p, 0.0, W, p);
+  svd_jacobi(c, Hp, p, p, Up, Sp, Vp, true, 0);  // |λ| descending, as eigh_small sorts
+  k_eig_from_svd<<<(unsigned)((p * 32 + 255) / 256), 256, 0, c->stream>>>(Up, Vp, Sp, (int)p, lam);
+  count_launch(c);
+  gemm_f64(c, 'N', 'N', p, p, p, 1.0, W0, p, Vp, p, 0.0, W, p);
 }
 
 MixedRun ctmrg_run_mixed(tnad_ctx* c, const double* a_, int d, int chi, double* C, double* T, double tol, int maxit,

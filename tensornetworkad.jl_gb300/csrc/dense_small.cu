@@ -345,9 +345,9 @@ __global__ void k_polar_ns(const double* __restrict__ X, int m, int iters, doubl
       float t = 0.f;
       for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t = fmaxf(t, red[w]);
       red[0] = t;
-      // all iterations run: the FP32 iterate must reach the polar factor to FP32
-      // accuracy (stopping at an orthogonality of 1e-5 and polishing in FP64
-      // gave a visibly worse-conditioned fixed-point adjoint)
+      // all iterations run: stopping once AᵀA is at FP32 rounding (and polishing
+      // in FP64) changed the converged gauge enough to make the fixed-point
+      // adjoint's GMRES several times slower
       done = it == iters ? 1 : 0;
     }
     __syncthreads();

@@ -483,6 +483,7 @@ void svd_jacobi(tnad_ctx* c, const double* A, int64_t m, int64_t n, double* U, d
     gemm_f64(c, 'N', 'N', m, n, n, 1.0, A, m, Vw, n, 0.0, W, m);
   }
   SweepGraph<double> sweep64;
+  int prev_rot = 0;
   for (int sweep = 0; sweep < kMaxSweeps && !converged; ++sweep) {
     // Purely relative sweeps first (rel_sweeps of them): they drive null and
     // noise-level columns to exact orthogonality (the triplets trg_svd's √s
@@ -507,7 +508,13 @@ void svd_jacobi(tnad_ctx* c, const double* A, int64_t m, int64_t n, double* U, d
     TNAD_CK(cudaMemcpyAsync(c->h_flag, flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     TNAD_CK(cudaStreamSynchronize(c->stream));
     if (trace) std::fprintf(stderr, "[tnad trace] svd n=%lld fp64 sweep %d rotations %d\n", (long long)n, sweep, c->h_flag[0]);
-    if (c->h_flag[0] == 0) converged = true;
+    const int rot = c->h_flag[0];
+    // symmetric, LAPACK-level rule: a sweep that only rotated a few pairs, far
+    // fewer than the sweep before (quadratic regime), applied only tiny angles
+    // and needs no further check sweep
+    if (rot == 0 || (symmetric && rel_sweeps == 0 && sweep > 0 && rot <= n / 8 && 8 * rot <= prev_rot))
+      converged = true;
+    prev_rot = rot;
   }
   TNAD_REQUIRE(converged, TNAD_ERR_NOT_CONVERGED, "svd_jacobi: no convergence within the sweep cap");
   k_colnorms<<<(int)((n * 32 + 255) / 256), 256, 0, c->stream>>>(W, Vw, m, n, s, sg);

@@ -328,14 +328,29 @@ __global__ void k_polar_ns(const double* __restrict__ X, int m, int iters, doubl
   __syncthreads();
   float worst = 0.f;
   for (int it = 0; it <= iters; ++it) {
-    // G = AᵀA, and how far it is from I
+    // G = AᵀA, and how far it is from I; each thread owns a 2×2 block of G
+    // (half the shared-memory loads per multiply-add of one element per thread)
     float dev = 0.f;
-    for (int e = threadIdx.x; e < mm; e += blockDim.x) {
-      const int i = e % m, j = e / m;
-      float acc = 0.f;
-      for (int k = 0; k < m; ++k) acc += A[k + i * ld] * A[k + j * ld];
-      G[i + j * ld] = acc;
-      dev = fmaxf(dev, fabsf(acc - (i == j ? 1.f : 0.f)));
+    const int mh = (m + 1) >> 1;
+    for (int e = threadIdx.x; e < mh * mh; e += blockDim.x) {
+      const int i0 = 2 * (e % mh), j0 = 2 * (e / mh);
+      const int i1 = min(i0 + 1, m - 1), j1 = min(j0 + 1, m - 1);
+      float g00 = 0.f, g01 = 0.f, g10 = 0.f, g11 = 0.f;
+      for (int k = 0; k < m; ++k) {
+        const float a0 = A[k + i0 * ld], a1 = A[k + i1 * ld], b0 = A[k + j0 * ld], b1 = A[k + j1 * ld];
+        g00 += a0 * b0;
+        g01 += a0 * b1;
+        g10 += a1 * b0;
+        g11 += a1 * b1;
+      }
+      G[i0 + j0 * ld] = g00;
+      G[i0 + j1 * ld] = g01;
+      G[i1 + j0 * ld] = g10;
+      G[i1 + j1 * ld] = g11;
+      dev = fmaxf(dev, fabsf(g00 - (i0 == j0 ? 1.f : 0.f)));
+      dev = fmaxf(dev, fabsf(g01 - (i0 == j1 ? 1.f : 0.f)));
+      dev = fmaxf(dev, fabsf(g10 - (i1 == j0 ? 1.f : 0.f)));
+      dev = fmaxf(dev, fabsf(g11 - (i1 == j1 ? 1.f : 0.f)));
     }
     for (int o = 16; o > 0; o >>= 1) dev = fmaxf(dev, __shfl_xor_sync(0xffffffffu, dev, o));
     __syncthreads();
@@ -353,12 +368,22 @@ __global__ void k_polar_ns(const double* __restrict__ X, int m, int iters, doubl
     __syncthreads();
     worst = red[0];
     if (done) break;
-    // B = A·(1.5 I − 0.5 G)
-    for (int e = threadIdx.x; e < mm; e += blockDim.x) {
-      const int i = e % m, j = e / m;
-      float acc = 1.5f * A[i + j * ld];
-      for (int k = 0; k < m; ++k) acc -= 0.5f * A[i + k * ld] * G[k + j * ld];
-      B[i + j * ld] = acc;
+    // B = A·(1.5 I − 0.5 G), 2×2 blocks per thread
+    for (int e = threadIdx.x; e < mh * mh; e += blockDim.x) {
+      const int i0 = 2 * (e % mh), j0 = 2 * (e / mh);
+      const int i1 = min(i0 + 1, m - 1), j1 = min(j0 + 1, m - 1);
+      float b00 = 0.f, b01 = 0.f, b10 = 0.f, b11 = 0.f;
+      for (int k = 0; k < m; ++k) {
+        const float a0 = A[i0 + k * ld], a1 = A[i1 + k * ld], g0 = G[k + j0 * ld], g1 = G[k + j1 * ld];
+        b00 += a0 * g0;
+        b01 += a0 * g1;
+        b10 += a1 * g0;
+        b11 += a1 * g1;
+      }
+      B[i0 + j0 * ld] = 1.5f * A[i0 + j0 * ld] - 0.5f * b00;
+      B[i0 + j1 * ld] = 1.5f * A[i0 + j1 * ld] - 0.5f * b01;
+      B[i1 + j0 * ld] = 1.5f * A[i1 + j0 * ld] - 0.5f * b10;
+      B[i1 + j1 * ld] = 1.5f * A[i1 + j1 * ld] - 0.5f * b11;
     }
     __syncthreads();
     float* t = A;

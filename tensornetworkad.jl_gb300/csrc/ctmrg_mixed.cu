@@ -185,35 +185,18 @@ __global__ void k_eig_from_svd(const double* __restrict__ U, const double* __res
   if (lane == 0) lam[w] = d < 0.0 ? -S[w] : S[w];
 }
 
-// FP64 eigendecomposition of the p×p Rayleigh–Ritz matrix H: the FP32 Jacobi
-// solver first, its eigenvectors re-orthogonalised in FP64 (Newton–Schulz),
-// then the nearly diagonal H' = WᵀHW finished by the multi-CTA FP64 Jacobi
-// SVD (one CTA per column pair, sweeps replayed as CUDA graphs: GB300's FP64
-// pipe is too narrow for a one-SM FP64 solver), W ← W·V'.
-void eigh_small_refined(tnad_ctx* c, const double* H, int64_t p, double* W, double* lam, int* dev_info) {
+// FP64 eigendecomposition of the p×p Rayleigh–Ritz matrix H in the FP64 phase,
+// through the multi-CTA FP64 Jacobi SVD (one CTA per column pair, sweeps
+// replayed as CUDA graphs; GB300's FP64 pipe is too narrow for a one-SM FP64
+// solver).  By then Q carries the previous Ritz basis, so H is nearly diagonal
+// and a few sweeps suffice; λ_i = σ_i·sign(u_i·v_i), ordered by |λ| descending.
+void eigh_small_fp64(tnad_ctx* c, const double* H, int64_t p, double* W, double* lam) {
   WsScope scope(c);
-  double* W0 = ws_d(c, p * p);
-  double* G = ws_d(c, p * p);
-  double* T1 = ws_d(c, p * p);
-  double* Hp = ws_d(c, p * p);
   double* Up = ws_d(c, p * p);
   double* Sp = ws_d(c, p);
-  double* Vp = ws_d(c, p * p);
-  eigh_small_prec(c, true, H, p, W0, lam, 40, dev_info);
-  for (int it = 0; it < 2; ++it) {
-    gemm_f64(c, 'T', 'N', p, p, p, 1.0, W0, p, W0, p, 0.0, G, p);
-    copy_d2d(c, T1, W0, p * p);
-    gemm_f64(c, 'N', 'N', p, p, p, -0.5, W0, p, G, p, 1.5, T1, p);
-    copy_d2d(c, W0, T1, p * p);
-  }
-  gemm_f64(c, 'N', 'N', p, p, p, 1.0, H, p, W0, p, 0.0, T1, p);
-  gemm_f64(c, 'T', 'N', p, p, p, 1.0, W0, p, T1, p, 0.0, Hp, p);
-  k_symmetrize_small<<<nb(p * p), 256, 0, c->stream>>>(Hp, (int)p);
+  svd_jacobi(c, H, p, p, Up, Sp, W, true, 0);
+  k_eig_from_svd<<<(unsigned)((p * 32 + 255) / 256), 256, 0, c->stream>>>(Up, W, Sp, (int)p, lam);
   count_launch(c);
-  svd_jacobi(c, Hp, p, p, Up, Sp, Vp, true, 0);  // |λ| descending, as eigh_small sorts
-  k_eig_from_svd<<<(unsigned)((p * 32 + 255) / 256), 256, 0, c->stream>>>(Up, Vp, Sp, (int)p, lam);
-  count_launch(c);
-  gemm_f64(c, 'N', 'N', p, p, p, 1.0, W0, p, Vp, p, 0.0, W, p);
 }
 
 MixedRun ctmrg_run_mixed(tnad_ctx* c, const double* a_, int d, int chi, double* C, double* T, double tol, int maxit,
@@ -287,7 +270,7 @@ MixedRun ctmrg_run_mixed(tnad_ctx* c, const double* a_, int d, int chi, double* 
     k_symmetrize_small<<<nb(p * p), 256, 0, c->stream>>>(H, (int)p);
     count_launch(c);
     if (prec == TNAD_PREC_FP64)
-      eigh_small_refined(c, H, p, Wm, lam, c->d_flag + 17);
+      eigh_small_fp64(c, H, p, Wm, lam);
     else
       eigh_small_prec(c, true, H, p, Wm, lam, 40, c->d_flag + 17);
     if (tr.on()) {

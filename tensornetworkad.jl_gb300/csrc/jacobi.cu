@@ -122,13 +122,19 @@ __global__ void __launch_bounds__(128) k_jacobi_round_cta(T* __restrict__ W, T* 
   }
   T* wp = W + (int64_t)p * m;
   T* wq = W + (int64_t)q * m;
-  T x[R], y[R];
+  T* vp = V + (int64_t)p * n;
+  T* vq = V + (int64_t)q * n;
+  T x[R], y[R], vx[R], vy[R];
   T a = 0, b = 0, g = 0;
+  // V's columns are loaded up front with W's (n ≤ m here): their latency
+  // overlaps the reduction instead of following the rotation decision
 #pragma unroll
   for (int k = 0; k < R; ++k) {
     const int64_t i = threadIdx.x + (int64_t)k * 128;
     x[k] = i < m ? wp[i] : (T)0;
     y[k] = i < m ? wq[i] : (T)0;
+    vx[k] = i < n ? vp[i] : (T)0;
+    vy[k] = i < n ? vq[i] : (T)0;
   }
 #pragma unroll
   for (int k = 0; k < R; ++k) {
@@ -178,12 +184,13 @@ __global__ void __launch_bounds__(128) k_jacobi_round_cta(T* __restrict__ W, T* 
       wq[i] = sn * x[k] + cs * y[k];
     }
   }
-  T* vp = V + (int64_t)p * n;
-  T* vq = V + (int64_t)q * n;
-  for (int64_t i = threadIdx.x; i < n; i += 128) {
-    const T xv = vp[i], yv = vq[i];
-    vp[i] = cs * xv - sn * yv;
-    vq[i] = sn * xv + cs * yv;
+#pragma unroll
+  for (int k = 0; k < R; ++k) {
+    const int64_t i = threadIdx.x + (int64_t)k * 128;
+    if (i < n) {
+      vp[i] = cs * vx[k] - sn * vy[k];
+      vq[i] = sn * vx[k] + cs * vy[k];
+    }
   }
 }
 

@@ -1,7 +1,7 @@
 """The CPU oracle pinned against the reference's published values and tests.
 
 These are the checks that make the oracle trustworthy before it is used to
-judge the GPU path (restatements of test/trg.jl, test/svd.jl, test/ctmrg.jl,
+check the GPU path (restatements of test/trg.jl, test/svd.jl, test/ctmrg.jl,
 test/fixedpoint.jl, test/autodiff.jl, test/exampletensors.jl and the README).
 """
 import json

@@ -302,8 +302,8 @@ def run_gb300(args):
         "e2e": {"value": round(t_e2e, 6), "unit": "s", "h2d_bytes_per_step": 8 * (nA + 16),
                 "d2h_bytes_per_step": 8 * (nA + 1)},
         "gpu_launches": int(launches),
-        "roofline": {"kernel": "k_jacobi_round_cta (FP64 one-sided Jacobi round, full SVD of the 1024x1024 corner "
-                               "for the implicit adjoint)",
+        "roofline": {"kernel": "k_jacobi_round_cta<8, double> (FP64 one-sided Jacobi round, polishing sweeps of "
+                               "the full SVD of the 1024x1024 corner for the implicit adjoint)",
                      "bound": "fp64", "achieved": round(ach_fp64, 4) if ach_fp64 else None,
                      "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
                      "frac": round(ach_fp64 / FP64_NOMINAL_TFLOPS, 4) if ach_fp64 else None,

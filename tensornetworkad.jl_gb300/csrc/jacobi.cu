@@ -505,7 +505,10 @@ void svd_jacobi(tnad_ctx* c, const double* A, int64_t m, int64_t n, double* U, d
     // and one plane rotation of W (6m) and V (6n)
     const double round_flops = (double)(n / 2) * (12.0 * (double)m + 6.0 * (double)n);
     if (m <= 2048) {
-      sweep64.run(c, "jacobi_round", W, Vw, m, n, NP, tol, ae, fro2, flag, round_flops);
+      // timer family: the large decompositions (the adjoint's χd×χd corner) apart
+      // from the p×p Rayleigh–Ritz ones
+      sweep64.run(c, n >= kPrecondMinN ? "jacobi_round" : "jacobi_round_small", W, Vw, m, n, NP, tol, ae, fro2,
+                  flag, round_flops);
     } else {
       TNAD_CK(cudaMemsetAsync(flag, 0, sizeof(int), c->stream));
       for (int r = 0; r < NP - 1; ++r) {

@@ -169,7 +169,8 @@ FixedPointInfo ctmrg_fixedpoint_adjoint(tnad_ctx* c, int prec, const double* a_,
   double rel = 1.0;
   if (prec != TNAD_PREC_FP64) {
     // GMRES with iterative refinement: the tensor-core operator solves for the
-    // correction (to 1e-3, well above its ~1e-5 noise floor) and the FP64
+    // correction (to 1e-3, well above its ~1e-5 noise floor; 1e-4 cost more
+    // tensor-core iterations than the FP64 residual it saved) and the FP64
     // operator only forms the residual, once per refinement.
     tr.mark("gmres_tf32");
     WsScope s3(c);

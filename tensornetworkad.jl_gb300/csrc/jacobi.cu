@@ -481,13 +481,16 @@ void svd_jacobi(tnad_ctx* c, const double* A, int64_t m, int64_t n, double* U, d
     }
     k_to_double<<<(int)nb_nn, 256, 0, c->stream>>>(V32, n * n, Vw);
     count_launch(c);
-    // V ← V·(3I − VᵀV)/2, three times: orthogonal to FP64 rounding
+    // V ← V·(3I − VᵀV)/2, three times: orthogonal to FP64 rounding.  The first
+    // step (from ‖VᵀV − I‖ ~ 1e-5) runs its products on the tensor cores
+    // (3xTF32, error ~1e-7); the two FP64 steps after it square the error away.
     double* G = ws_d(c, n * n);
     double* V2 = ws_d(c, n * n);
     for (int it = 0; it < 3; ++it) {
-      gemm_f64(c, 'T', 'N', n, n, n, 1.0, Vw, n, Vw, n, 0.0, G, n);
+      const int pr = (it == 0 && c->tc_ok) ? TNAD_PREC_TF32X3 : TNAD_PREC_FP64;
+      gemm(c, pr, 'T', 'N', n, n, n, 1.0, Vw, n, Vw, n, 0.0, G, n);
       copy_d2d(c, V2, Vw, n * n);
-      gemm_f64(c, 'N', 'N', n, n, n, -0.5, Vw, n, G, n, 1.5, V2, n);
+      gemm(c, pr, 'N', 'N', n, n, n, -0.5, Vw, n, G, n, 1.5, V2, n);
       copy_d2d(c, Vw, V2, n * n);
     }
     gemm_f64(c, 'N', 'N', m, n, n, 1.0, A, m, Vw, n, 0.0, W, m);

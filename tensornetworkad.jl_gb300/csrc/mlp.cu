@@ -41,6 +41,7 @@ struct tnad_mlp {
   float* DX = nullptr;    // resident training set (tnad_mlp_set_data): n_in × n_data
   float* DY = nullptr;    //                                            n_out × n_data
   int64_t n_data = 0;
+  ~tnad_mlp();  // releases every device buffer (also on a failed create)
 };
 
 namespace tnad {
@@ -435,16 +436,16 @@ extern "C" int tnad_mlp_create(tnad_ctx* c, int n_in, int width, int n_out, uint
   API_END(c)
 }
 
-extern "C" void tnad_mlp_free(tnad_mlp* net) {
-  if (!net) return;
-  cudaSetDevice(net->device);
+tnad_mlp::~tnad_mlp() {
+  cudaSetDevice(device);
   cudaDeviceSynchronize();
-  free_batch_buffers(net);
-  for (float* p : {net->P, net->G, net->M1, net->M2, net->DX, net->DY})
+  free_batch_buffers(this);
+  for (float* p : {P, G, M1, M2, DX, DY})
     if (p) cudaFree(p);
-  if (net->red) cudaFree(net->red);
-  delete net;
+  if (red) cudaFree(red);
 }
+
+extern "C" void tnad_mlp_free(tnad_mlp* net) { delete net; }
 
 extern "C" int64_t tnad_mlp_param_count(const tnad_mlp* net) { return net ? net->n_params : 0; }
 

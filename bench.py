@@ -233,8 +233,7 @@ def run_gb300(args):
         sol.device()
     torch.cuda.synchronize()
     barrier(dist)
-    # timed region: K solves with device-resident inputs (no kernel timer: its
-    # event records would keep the Jacobi sweeps out of their CUDA graphs)
+    # timed region: K solves with device-resident inputs (no kernel timer)
     l0 = c.launches
     errs, stats = [], []
     with Clocks(local) as clk:
@@ -253,7 +252,9 @@ def run_gb300(args):
     launches = (c.launches - l0) // args.steps
     t_dev = max_over_ranks(dist, ev0.elapsed_time(ev1) / 1e3 / args.steps)
     # one extra solve per kernel family with its launches bracketed by CUDA
-    # events on the library's stream (launched directly, not from a graph)
+    # events on the library's stream (a Jacobi sweep replayed as a CUDA graph
+    # is bracketed as a whole: its average launch duration includes the
+    # graph's gaps between rounds)
     fam = {}
     for name in ("jacobi_round", "jacobi_round_f32", "gemm_tf32x3"):
         kernel_timer(c, name)

@@ -153,6 +153,7 @@ static void kt_clear(tnad_ctx* c) {
   }
   c->kt_ev.clear();
   c->kt_work = 0.0;
+  c->kt_launches = 0;
 }
 
 extern "C" int tnad_ctx_kernel_timer(tnad_ctx* c, const char* name) {
@@ -173,7 +174,7 @@ extern "C" int tnad_ctx_kernel_timer_read(tnad_ctx* c, int64_t* launches, double
     float t = 0.f;
     if (cudaEventElapsedTime(&t, p.first, p.second) == cudaSuccess) ms += t;
   }
-  if (launches) *launches = (int64_t)c->kt_ev.size();
+  if (launches) *launches = c->kt_launches;
   if (total_ms) *total_ms = ms;
   if (work) *work = c->kt_work;
   return TNAD_OK;

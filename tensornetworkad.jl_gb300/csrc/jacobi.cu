@@ -211,8 +211,7 @@ void jacobi_round_launch(tnad_ctx* c, T* W, T* V, int64_t m, int64_t n, int r, i
 
 // One Jacobi sweep (flag reset + the NP−1 rounds) recorded once as a CUDA
 // graph and replayed for every sweep: the rounds are short kernels whose
-// launch cost is comparable to their run time.  Sweeps bracketed by the kernel
-// timer (event records cannot go into the graph) and very small matrices are
+// launch cost is comparable to their run time.  Very small matrices are
 // launched directly.
 template <typename T>
 struct SweepGraph {
@@ -223,8 +222,7 @@ struct SweepGraph {
   }
   void run(tnad_ctx* c, const char* family, T* W, T* V, int64_t m, int64_t n, int NP, double tol, double ae,
            const double* fro2, int* flag, double round_flops) {
-    const bool timed = !c->ktimer.empty() && c->ktimer == family;
-    if (timed || NP < 64) {
+    if (NP < 64) {
       TNAD_CK(cudaMemsetAsync(flag, 0, sizeof(int), c->stream));
       for (int r = 0; r < NP - 1; ++r) {
         KernelTimer kt(c, family, round_flops);
@@ -250,6 +248,9 @@ struct SweepGraph {
         if (e != cudaSuccess) fail(TNAD_ERR_CUDA, std::string("jacobi sweep graph: ") + cudaGetErrorString(e));
         ae_ = ae;
       }
+      // timed as one bracket around the replayed sweep (events cannot go inside
+      // the graph): the average launch duration includes the graph's own gaps
+      KernelTimer kt(c, family, round_flops * (NP - 1), NP - 1);
       TNAD_CK(cudaGraphLaunch(exec, c->stream));
     }
     count_launch(c, NP - 1);

@@ -87,6 +87,7 @@ struct tnad_ctx {
   std::string ktimer;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> kt_ev;
   double kt_work = 0.0;
+  int64_t kt_launches = 0;  // kernel launches inside the timed brackets
   // learned warm start (tnad_ctx_set_warm_start): network, the (D, s, χ) it
   // was trained for, and the outcome of the last energy call that used it
   tnad_mlp* warm_net = nullptr;
@@ -113,18 +114,19 @@ class PhaseTrace {
   std::vector<std::pair<const char*, cudaEvent_t>> ev_;
 };
 
-// Brackets one launch of kernel family `name` with CUDA events when the
-// context's kernel timer is set to that family.
+// Brackets one launch (or a graph of `launches` launches) of kernel family
+// `name` with CUDA events when the context's kernel timer is set to that family.
 struct KernelTimer {
   tnad_ctx* c;
   cudaEvent_t e1 = nullptr;
-  KernelTimer(tnad_ctx* ctx, const char* name, double work) : c(ctx) {
+  KernelTimer(tnad_ctx* ctx, const char* name, double work, int64_t launches = 1) : c(ctx) {
     if (c->ktimer.empty() || c->ktimer != name) return;
     cudaEvent_t e0;
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return;
     cudaEventRecord(e0, c->stream);
     c->kt_ev.push_back({e0, e1});
     c->kt_work += work;
+    c->kt_launches += launches;
   }
   ~KernelTimer() {
     if (e1) cudaEventRecord(e1, c->stream);

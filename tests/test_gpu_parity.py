@@ -257,3 +257,18 @@ def test_shape_errors(tn):
         tn.energy(tn.hamiltonian(tn.Heisenberg()), np.zeros((2, 3, 2, 2, 2)), 4, 1e-8, 10)
     with pytest.raises(tn.DimensionMismatch):
         tn.trg(np.zeros((2, 2, 3, 2)), 4, 2)
+
+
+@pytest.mark.parametrize("budget", [0, 200_000])
+def test_unrolled_gradient_recomputes_steps_beyond_the_tape_budget(tn, orc, budget):
+    """Unrolled reverse with a tape budget too small for the per-step
+    decompositions (none kept, or only the first few): the missing steps are
+    recomputed from the (C, T) checkpoints and the gradient is unchanged."""
+    h = tn.hamiltonian(tn.Heisenberg())
+    A = orc.ipeps_uniform(2, 2, 5)
+    full = tn.default_opts(prec=0, solver=0, adjoint=0)
+    E0, g0 = tn.energy_and_gradient(h, tn.SquareIPEPS(A), 12, 1e-12, 200, full)
+    small = tn.default_opts(prec=0, solver=0, adjoint=0, tape_budget=budget)
+    E1, g1 = tn.energy_and_gradient(h, tn.SquareIPEPS(A), 12, 1e-12, 200, small)
+    assert E1 == E0
+    assert rel(g1, g0) < 1e-12

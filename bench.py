@@ -58,10 +58,9 @@ def parse():
 
 
 def workload_input(w):
-    from oracle import tnad_oracle as orc  # seeded input recipe only (NumPy default_rng)
+    import __graft_entry__ as ge
 
-    return orc.ipeps_uniform(w["D"], 2, w["seed"]) if w["recipe"] == "uniform" else \
-        orc.ipeps_normal_maxabs(w["D"], 2, w["seed"])
+    return ge.load_package().site_tensor(w["recipe"], w["D"], 2, w["seed"])
 
 
 def plain_tol(w):
@@ -471,6 +470,69 @@ def run_learned(args):
     print(json.dumps(line), flush=True)
 
 
+def run_learned_headline(args):
+    """Learned warm start on the headline configuration (D=4, χ=64, N(0,1)
+    max-abs-normalised site tensors, Heisenberg): targets from the mixed CTMRG
+    on n_train tensors of that recipe (seeds other than the workload's), the
+    network trained on the GPU, then the energy+gradient solve of the bench
+    workload tensor (seed 0) timed from the learned start and from :raw, and
+    CTMRG steps of the energy on held-out tensors of the same recipe."""
+    import importlib
+
+    import torch
+    import __graft_entry__ as ge
+
+    tn = ge.load_package()
+    wl = importlib.import_module(tn.__name__ + ".learned")
+    w = ESTAR["heisenberg_D4_chi64"]
+    D, s, chi = 4, 2, 64
+    h = tn.hamiltonian(tn.Heisenberg())
+    t0 = time.perf_counter()
+    train = [tn.site_tensor("normal_maxabs", D, s, 1000 + i) for i in range(args.n_train)]
+    samples = wl.make_samples(train, h, chi, 1e-8, 400, tn.mixed_opts(), threads=args.threads)
+    t1 = time.perf_counter()
+    X, Y = wl.stack(samples)
+    net = wl.WarmStartNet(D, s, chi, width=512, seed=1)
+    info = net.fit(X, Y, steps=args.train_steps, batch=64, lr=1e-3, weight_decay=1e-4,
+                   log_every=max(1, args.train_steps // 6))
+    net.attach()
+    # the bench workload: energy + gradient, learned start vs :raw, device-resident inputs
+    res = {}
+    for name, warm in (("cold", tn._lib.WARM_NONE), ("learned", tn._lib.WARM_LEARNED)):
+        sol = Solver(tn, w, "mixed")
+        sol.opts_d.warm_start = warm
+        sol.device()
+        ts, stats, errs, status = [], None, [], []
+        for _ in range(max(args.steps, 1)):
+            torch.cuda.synchronize()
+            ta = time.perf_counter()
+            E, stats = sol.device()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - ta)
+            errs.append(abs(E - w["E_star"]))
+            status.append(wl.warm_start_status())
+        res[name] = {"s_per_solve": round(min(ts), 4), "ctmrg_steps": stats["steps"], "fp64_steps": stats["fp64_steps"],
+                     "fixedpoint_iters": stats["fp_iters"], "delta_E": max(errs), "warm_status": status[-1]}
+    held = [tn.site_tensor("normal_maxabs", D, s, 5000 + i) for i in range(args.n_held)]
+    r = wl.compare_starts(held, h, chi, 1e-8, 400, tn.mixed_opts)
+    line = {
+        "metric": "learned warm start on the headline workload (Heisenberg iPEPS D=4, chi=64): energy+gradient "
+                  "time to |dE|<=1e-8, learned start vs :raw",
+        "value": res["learned"]["s_per_solve"], "unit": "s", "higher_is_better": False,
+        "cold": res["cold"], "learned": res["learned"],
+        "speedup": round(res["cold"]["s_per_solve"] / res["learned"]["s_per_solve"], 3),
+        "held_out": {"n": len(held), "cold_steps": round(float(r["cold_steps"].mean()), 2),
+                     "warm_steps": round(float(r["warm_steps"].mean()), 2),
+                     "same_fixed_point": round(float(np.mean(r["dE"] <= 1e-8)), 3),
+                     "judge_kept": round(float(np.mean(r["status"] == 1)), 3)},
+        "train": {"n": len(samples), "seconds": round(info["seconds"], 2), "targets_s": round(t1 - t0, 1),
+                  "loss_std_final": round(info["loss_std"], 5), "steps": args.train_steps},
+        "config": {"workload": "learned_D4_chi64", "D": D, "chi": chi, "width": 512, "layers": 3},
+        "dtype": "bf16 network, mixed TF32X3/FP64 CTMRG", "data": "synthetic",
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_profile(args):
     import importlib
 
@@ -499,6 +561,8 @@ if __name__ == "__main__":
         run_profile(a)
     elif a.impl == "reference":
         run_reference(a)
+    elif a.workload == "learned_D4_chi64":
+        run_learned_headline(a)
     elif a.workload.startswith("learned"):
         run_learned(a)
     else:

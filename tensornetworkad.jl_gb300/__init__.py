@@ -472,6 +472,19 @@ __all__ = [
 # ---------------------------------------------------------------------------
 
 
+def site_tensor(recipe: str, D: int, s: int, seed: int) -> np.ndarray:
+    """Seeded synthetic site tensors of the benchmark workloads (NumPy default_rng):
+    "uniform" — entries uniform in [0, 1); "normal_maxabs" — N(0, 1) entries divided by
+    the largest |entry|."""
+    rng = np.random.default_rng(seed)
+    if recipe == "uniform":
+        return np.asfortranarray(rng.random((D, D, D, D, s)))
+    if recipe == "normal_maxabs":
+        x = rng.standard_normal((D, D, D, D, s))
+        return np.asfortranarray(x / np.abs(x).max())
+    raise ValueError(f"unknown site-tensor recipe {recipe!r}")
+
+
 def gemm(A, B, ta="N", tb="N", alpha=1.0, beta=0.0, Cin=None, prec=L.PREC_FP64):
     """alpha·op(A)·op(B) + beta·C on the GPU (column-major, FP64 or 3xTF32)."""
     A, B = farr(A), farr(B)

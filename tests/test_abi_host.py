@@ -72,3 +72,9 @@ def test_no_cpu_fallback_without_gpu(tn):
         pytest.skip("GPU present")
     with pytest.raises(tn.TnadError):
         tn._lib.Context(0)
+
+
+def test_site_tensor_recipes_match_the_oracle_fixtures(tn, orc):
+    """The package's seeded workload inputs are the oracle's (the E* fixtures were made from those)."""
+    assert np.array_equal(tn.site_tensor("uniform", 3, 2, 0), orc.ipeps_uniform(3, 2, 0))
+    assert np.array_equal(tn.site_tensor("normal_maxabs", 4, 2, 0), orc.ipeps_normal_maxabs(4, 2, 0))

@@ -296,7 +296,9 @@ def run_gb300(args):
         "data": "synthetic: N(0,1) site tensor (NumPy seed 0), max-abs normalised, symmetrised",
         "config": {"workload": args.workload, "D": sol.D, "chi": sol.chi, "phys": sol.s, "mode": args.mode,
                    "stop_tol": sol.tol, "ctmrg_steps": stats[-1]["steps"], "fp64_steps": stats[-1]["fp64_steps"],
-                   "fixedpoint_iters": stats[-1]["fp_iters"], "parallelism": f"replicas x{world}",
+                   "fixedpoint_iters": stats[-1]["fp_iters"],
+                   "fixedpoint_residual": stats[-1].get("fixed_point_residual"),
+                   "parallelism": f"replicas x{world}",
                    "l2": "no flush: each solve runs ~10^4 launches over a <300 MB working set (L2/HBM resident)"},
         "delta_E": max(errs), "E": E, "E_star": w["E_star"],
         "e2e": {"value": round(t_e2e, 6), "unit": "s", "h2d_bytes_per_step": 8 * (nA + 16),
@@ -512,7 +514,10 @@ def run_learned_headline(args):
             errs.append(abs(E - w["E_star"]))
             status.append(wl.warm_start_status())
         res[name] = {"s_per_solve": round(min(ts), 4), "ctmrg_steps": stats["steps"], "fp64_steps": stats["fp64_steps"],
-                     "fixedpoint_iters": stats["fp_iters"], "delta_E": max(errs), "warm_status": status[-1]}
+                     "fixedpoint_iters": stats["fp_iters"], "delta_E": max(errs), "warm_status": status[-1],
+                     "grad": sol.g_d.cpu().numpy()}
+    gc, gl = res["cold"].pop("grad"), res["learned"].pop("grad")
+    res["learned"]["grad_rel_diff_vs_cold"] = float(np.linalg.norm(gl - gc) / np.linalg.norm(gc))
     held = [tn.site_tensor("normal_maxabs", D, s, 5000 + i) for i in range(args.n_held)]
     r = wl.compare_starts(held, h, chi, 1e-8, 400, tn.mixed_opts)
     line = {

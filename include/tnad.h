@@ -212,6 +212,12 @@ int tnad_energy_backward(tnad_ctx* ctx, tnad_tape* tape, double dE, double* dA);
    (the reference reports none of these). */
 int tnad_energy_stats(const tnad_tape* tape, int* steps, int* fp64_steps, int* switch_step, int* fp_iters,
                       double* last_diff, double* fp_residual);
+/* After a fixed-point tnad_energy_backward: ‖f(x*) − x*‖/‖x*‖ of the gauge-aligned
+   CTMRG step at the converged environment.  The implicit adjoint assumes x* is
+   a fixed point; a residual well above the stop tolerance (the aligned gauge
+   did not lock) flags a gradient that should not be trusted.  No reference
+   counterpart. */
+int tnad_energy_fixed_point_residual(const tnad_tape* tape, double* residual);
 
 /* -------- learned warm start (no reference counterpart) --------
    A 3-layer perceptron n_in → width → width → n_out (ReLU between layers) that

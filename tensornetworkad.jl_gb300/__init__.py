@@ -393,7 +393,11 @@ def tape_stats(tape) -> dict:
     if rc != 0:
         raise TnadError(rc, "tnad_energy_stats")
     keys = ["steps", "fp64_steps", "switch_step", "fp_iters", "last_diff", "fp_residual"]
-    return {k: v.value for k, v in zip(keys, vals)}
+    out = {k: v.value for k, v in zip(keys, vals)}
+    r = C.c_double()
+    if tape.c.lib.tnad_energy_fixed_point_residual(tape.h, C.byref(r)) == 0:
+        out["fixed_point_residual"] = r.value
+    return out
 
 
 def mixed_opts(ladder_tol: float = 1e-5, fp_tol: float = 1e-9, fp_maxit: int = 200, **kw) -> L.Opts:

@@ -86,6 +86,7 @@ SIGNATURES = {
                               DP, IP, DP, DP, C.POINTER(VP)]),
     "tnad_energy_backward": (C.c_int, [VP, VP, C.c_double, DP]),
     "tnad_energy_stats": (C.c_int, [VP, IP, IP, IP, IP, DP, DP]),
+    "tnad_energy_fixed_point_residual": (C.c_int, [VP, DP]),
     "tnad_mlp_create": (C.c_int, [VP, C.c_int, C.c_int, C.c_int, C.c_uint64, C.POINTER(VP)]),
     "tnad_gemm_bf16": (C.c_int, [VP, C.c_char, C.c_char, C.c_int64, C.c_int64, C.c_int64, C.c_float, FP, C.c_int64,
                                  FP, C.c_int64, C.c_float, FP, C.c_int64]),

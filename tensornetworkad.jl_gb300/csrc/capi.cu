@@ -435,3 +435,9 @@ extern "C" int tnad_energy_stats(const tnad_tape* t, int* steps, int* fp64_steps
   if (fp_residual) *fp_residual = e.fp_residual;
   return TNAD_OK;
 }
+
+extern "C" int tnad_energy_fixed_point_residual(const tnad_tape* t, double* residual) {
+  if (!t || t->kind != 3 || !t->en || !residual) return TNAD_ERR_STATE;
+  *residual = t->en->fp_fixed_point_residual;
+  return TNAD_OK;
+}

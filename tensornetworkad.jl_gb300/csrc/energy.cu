@@ -344,6 +344,7 @@ void energy_bwd(tnad_ctx* c, EnergyTape& tp, double dE, double* dA) {
         ctmrg_fixedpoint_adjoint(c, pr, tp.a, d, chi, tp.C, tp.T, tp.zstar, dC, dT, dbulk, tp.fp_tol, tp.fp_maxit);
     tp.fp_iters = fi.iters;
     tp.fp_residual = fi.residual;
+    tp.fp_fixed_point_residual = fi.fixed_point_residual;
   } else {
     ctmrg_reverse(c, tp.ct, dC, dT, dbulk);
   }

@@ -17,6 +17,9 @@
 #include <cmath>
 #include <vector>
 
+#include <algorithm>
+#include <cstdio>
+
 #include "tnad_mixed.h"
 
 namespace tnad {
@@ -35,9 +38,17 @@ struct Op {
   const StepCache* cache;
   double* scratch_a;
   int64_t nCh, nx;
-  // w = v − (∂f/∂x)ᵀ v
+  double tsign;   // +1, or −1 when the step maps T* to −T* (see below)
+  double* sv;     // scratch for S·v
+  // w = v − (∂g/∂x)ᵀ v with g = S·f, S = diag(1 on C, tsign on T)
   void apply(const double* v, double* w, double* jt) const {
-    ctmrg_step_bwd(c, prec, a, d, chi, Cs, Ts, U, S, V, v, v + nCh, scratch_a, jt, jt + nCh, false, O, zref, cache);
+    const double* u = v;
+    if (tsign < 0.0) {
+      copy_d2d(c, sv, v, nx);
+      scale(c, nx - nCh, -1.0, sv + nCh);
+      u = sv;
+    }
+    ctmrg_step_bwd(c, prec, a, d, chi, Cs, Ts, U, S, V, u, u + nCh, scratch_a, jt, jt + nCh, false, O, zref, cache);
     copy_d2d(c, w, v, nx);
     axpby(c, nx, -1.0, jt, 1.0, w);
   }
@@ -167,6 +178,38 @@ FixedPointInfo ctmrg_fixedpoint_adjoint(tnad_ctx* c, int prec, const double* a_,
   FixedPointInfo info;
   const int m = 30;
   double rel = 1.0;
+  // The step is odd in T (T → −T gives C' → C', T' → −T'), so a converged run
+  // can sit on T* = −f_T(x*): C and the energy are converged but T flips sign
+  // every step.  Then x* is a fixed point of g = S·f with S = −1 on T, and the
+  // adjoint is taken for g.  The sign is only trusted when x* is a fixed point
+  // of g to ~1e-6 while it is not one of f.  (When neither holds — the aligned
+  // gauge has not locked, e.g. a truncation cut through a slowly decaying
+  // spectrum — the implicit adjoint's premise fails; the residuals are printed
+  // under TNAD_TRACE.)
+  double* sv = ws_d(c, nx);
+  StepCache cache64;  // FP64 forward intermediates of the step at x* (all FP64 operators share them)
+  step_cache_fill(c, TNAD_PREC_FP64, a_, d, chi, Cs, Ts, U, O, cache64);
+  double tsign = 1.0;
+  {
+    WsScope s1(c);
+    double* dd = ws_d(c, nTe);
+    const double nT = norm_host(c, Ts, nTe);
+    copy_d2d(c, dd, cache64.Tout, nTe);
+    axpby(c, nTe, -1.0, Ts, 1.0, dd);
+    const double r_plus = norm_host(c, dd, nTe) / nT;
+    copy_d2d(c, dd, cache64.Tout, nTe);
+    axpby(c, nTe, 1.0, Ts, 1.0, dd);
+    const double r_minus = norm_host(c, dd, nTe) / nT;
+    copy_d2d(c, dd, cache64.Cout, nCh);
+    axpby(c, nCh, -1.0, Cs, 1.0, dd);
+    const double r_c = norm_host(c, dd, nCh) / norm_host(c, Cs, nCh);
+    if (r_minus < 1e-6 && r_plus > 1e-2 && r_c < 1e-6) tsign = -1.0;
+    info.fixed_point_residual = std::max(r_c, tsign < 0.0 ? r_minus : r_plus);
+    if (tr.on())
+      std::fprintf(stderr, "[tnad trace] fixed point x*: |f_C - C|/|C| = %.3e  |f_T - T|/|T| = %.3e  |f_T + T|/|T| = %.3e\n",
+                   r_c, r_plus, r_minus);
+  }
+  info.tsign = tsign;
   if (prec != TNAD_PREC_FP64) {
     // GMRES with iterative refinement: the tensor-core operator solves for the
     // correction (to 1e-3, well above its ~1e-5 noise floor; 1e-4 cost more
@@ -174,11 +217,10 @@ FixedPointInfo ctmrg_fixedpoint_adjoint(tnad_ctx* c, int prec, const double* a_,
     // operator only forms the residual, once per refinement.
     tr.mark("gmres_tf32");
     WsScope s3(c);
-    StepCache cache_tc, cache64;
+    StepCache cache_tc;
     step_cache_fill(c, prec, a_, d, chi, Cs, Ts, U, O, cache_tc);
-    step_cache_fill(c, TNAD_PREC_FP64, a_, d, chi, Cs, Ts, U, O, cache64);
-    Op Atc{c, prec, a_, d, chi, Cs, Ts, U, S, V, O, zref, &cache_tc, scratch_a, nCh, nx};
-    Op A64{c, TNAD_PREC_FP64, a_, d, chi, Cs, Ts, U, S, V, O, zref, &cache64, scratch_a, nCh, nx};
+    Op Atc{c, prec, a_, d, chi, Cs, Ts, U, S, V, O, zref, &cache_tc, scratch_a, nCh, nx, tsign, sv};
+    Op A64{c, TNAD_PREC_FP64, a_, d, chi, Cs, Ts, U, S, V, O, zref, &cache64, scratch_a, nCh, nx, tsign, sv};
     info.iters += gmres(c, Atc, g, lam, m, std::max(tol, 1e-3), std::min(maxit, 40), &rel);
     tr.mark("refine");
     double* r = ws_d(c, nx);
@@ -205,15 +247,14 @@ FixedPointInfo ctmrg_fixedpoint_adjoint(tnad_ctx* c, int prec, const double* a_,
     // FP64 GMRES from the current λ to the requested tolerance
     tr.mark("gmres_f64");
     WsScope s3(c);
-    StepCache cache;
-    step_cache_fill(c, TNAD_PREC_FP64, a_, d, chi, Cs, Ts, U, O, cache);
-    Op A{c, TNAD_PREC_FP64, a_, d, chi, Cs, Ts, U, S, V, O, zref, &cache, scratch_a, nCh, nx};
+    Op A{c, TNAD_PREC_FP64, a_, d, chi, Cs, Ts, U, S, V, O, zref, &cache64, scratch_a, nCh, nx, tsign, sv};
     info.iters += gmres(c, A, g, lam, m, tol, maxit, &rel);
   }
   info.residual = rel;
-  // ā += (∂f/∂a)ᵀ λ
+  // ā += (∂g/∂a)ᵀ λ = (∂f/∂a)ᵀ S·λ
   tr.mark("pullback_a");
   double* jt = ws_d(c, nx);
+  if (tsign < 0.0) scale(c, nx - nCh, -1.0, lam + nCh);
   ctmrg_step_bwd(c, TNAD_PREC_FP64, a_, d, chi, Cs, Ts, U, S, V, lam, lam + nCh, dbulk, jt, jt + nCh, true, O, zref);
   return info;
 }

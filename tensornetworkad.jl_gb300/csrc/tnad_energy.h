@@ -19,6 +19,7 @@ struct EnergyTape {
   int fp64_steps = 0, switch_step = 0;  // mixed solver: FP64 polishing steps, ladder hand-over
   int fp_iters = 0;                     // fixed-point adjoint iterations used
   double fp_residual = 0.0, fp_tol = 1e-10, last_diff = 0.0;
+  double fp_fixed_point_residual = 0.0;  // ‖f(x*) − x*‖/‖x*‖ of the aligned step (implicit adjoint)
   int fp_maxit = 200;
   double E = 0.0;
   DevPool pool;

@@ -30,6 +30,8 @@ MixedRun ctmrg_run_mixed(tnad_ctx* c, const double* a, int d, int chi, double* C
 struct FixedPointInfo {
   int iters = 0;
   double residual = 0.0;
+  double tsign = 1.0;  // −1: the converged T flips sign every step
+  double fixed_point_residual = 0.0;  // ‖g(x*) − x*‖/‖x*‖ of the aligned step at x*
 };
 
 // Implicit adjoint at a converged environment (C*, T*) of bulk a: given the

@@ -38,6 +38,8 @@ def test_mixed_energy_and_fixedpoint_gradient_D3_chi36(tn, orc):
     assert abs(E - E_r) < 1e-9
     assert rel(g, g_r) < 1e-5, st
     assert st["fp_iters"] >= 1
+    # the implicit adjoint's premise holds here: x* is a fixed point of the aligned step
+    assert st["fixed_point_residual"] < 1e-6, st
 
 
 def test_plain_fixedpoint_adjoint_matches_unrolled(tn, orc):

@@ -4,15 +4,19 @@
 // (p = χ + max(16, χ/2), so the lag rate is |λ_{p+1}/λ_χ| instead of
 // |λ_{χ+1}/λ_χ|).  Per step, with M = cp + cpᵀ and Q (n×p, orthonormal):
 //     Y = M·Q                       (tensor cores, 3xTF32)
-//     H = Qᵀ·Y, H = W·diag(θ)·Wᵀ    (Rayleigh–Ritz; one-CTA Jacobi, sorted by |θ|)
+//     H = Qᵀ·Y, H = W·diag(θ)·Wᵀ    (Rayleigh–Ritz, sorted by |θ|: one-CTA FP32
+//                                    Jacobi, or the multi-CTA FP64 Jacobi SVD)
 //     z = Q·W[:, 1:χ]               (Ritz vectors: the projector of this step)
+//     z ← z·polar(zᵀ·z_prev)        (gauge alignment with the previous projector)
 //     Q ← CholeskyQR2(Y·W)          (power step on the Ritz basis, order kept)
 // The dense contractions run at TF32X3 until the Ritz-value residual reaches
 // ladder_tol or stalls, then the same iteration continues in FP64 (DFMA GEMMs,
 // FP64 Jacobi) until ‖Δ(|θ|/|θ₁|)_{1:χ}‖₂ ≤ tol.  Any orthonormal basis of the
 // top-χ subspace gives a gauge-equivalent environment, so the fixed point is
-// the reference's; z columns are sign-aligned with the previous step's so that
-// the converged environment is a strict fixed point (used by the implicit adjoint).
+// the reference's.  The polar alignment keeps consecutive environments in one
+// gauge, which the implicit adjoint needs (x* = f(x*)); where the projector's
+// gauge near the χ cut keeps moving (D=4 workloads) that premise fails, and
+// tnad_energy_fixed_point_residual reports it.
 #include <cmath>
 #include <cstdio>
 #include <limits>

@@ -205,6 +205,23 @@ class Solver:
         return E, g, st
 
 
+def gradient_check(tn, sol, g_mixed, g_plain, step=1e-4, tol=1e-11):
+    """Directional derivative of the energy along a seeded unit direction v: the
+    mixed gradient and the plain FP64 path's (the reference's unrolled reverse)
+    against a central difference of the plain FP64 energy (stop rule tol)."""
+    v = np.random.default_rng(1).standard_normal(np.shape(sol.A))
+    v /= np.linalg.norm(v)
+    plain = tn.default_opts()
+    E = [tn.energy(sol.h, tn.SquareIPEPS(np.asfortranarray(sol.A + sg * step * v)), sol.chi, tol, sol.maxit, plain)
+         for sg in (1.0, -1.0)]
+    fd = (E[0] - E[1]) / (2 * step)
+    gm, gp = float(np.sum(g_mixed * v)), float(np.sum(g_plain * v))
+    return {"direction": "unit N(0,1) direction (NumPy seed 1)", "fd_step": step, "fd_stop_tol": tol,
+            "fd": fd, "mixed": gm, "mixed_rel_err": abs(gm - fd) / abs(fd),
+            "plain_unrolled": gp, "plain_unrolled_rel_err": abs(gp - fd) / abs(fd),
+            "mixed_vs_plain_rel_l2": float(np.linalg.norm(g_mixed - g_plain) / np.linalg.norm(g_plain))}
+
+
 def kernel_timer(c, name):
     c.check(c.lib.tnad_ctx_kernel_timer(c.h, name.encode()))
 
@@ -271,7 +288,7 @@ def run_gb300(args):
         E_h, g_h, st_h = sol.host()
     t_e2e = max_over_ranks(dist, (time.perf_counter() - t1) / args.steps)
     # the plain FP64 GPU path (full Jacobi SVD each step, unrolled reverse), one solve
-    plain = None
+    plain, grad_check = None, None
     if args.mode == "mixed" and not args.no_plain:
         ps = Solver(tn, w, "plain")
         t2 = time.perf_counter()
@@ -280,6 +297,8 @@ def run_gb300(args):
         tp_ = time.perf_counter() - t2
         plain = {"value": round(tp_, 4), "unit": "s", "ctmrg_steps": stp["steps"], "delta_E": abs(Ep - w["E_star"]),
                  "steps": 1, "warmup": 0}
+        if rank == 0:
+            grad_check = gradient_check(tn, sol, g_h, ps.g_d.cpu().numpy().reshape(np.shape(sol.A), order="F"))
     if rank != 0:
         return
     pk, pk_kind = peaks()
@@ -328,6 +347,8 @@ def run_gb300(args):
     }
     if plain:
         line["plain_fp64"] = plain
+    if grad_check:
+        line["gradient_check"] = grad_check
         line["speedup_vs_plain_fp64"] = round(plain["value"] / t_dev, 2)
     if not args.no_cpu_baseline:
         cb, need = oracle_sample(w)

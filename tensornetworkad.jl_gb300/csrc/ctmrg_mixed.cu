@@ -27,8 +27,6 @@ namespace tnad {
 
 void chol_inv_upper(tnad_ctx* c, const double* G, int64_t p, double* Rinv, int* dev_fail);
 void chol_inv_upper_f32(tnad_ctx* c, const double* G, int64_t p, double* Rinv, int* dev_fail);
-void eigh_small_prec(tnad_ctx* c, bool fp32, const double* A, int64_t p, double* W, double* lam, int max_sweeps,
-                     int* dev_info);
 void randn(tnad_ctx* c, double* x, int64_t n, uint64_t seed, double scale, bool accumulate,
            const double* dev_sumsq = nullptr);
 

@@ -143,12 +143,13 @@ __device__ __forceinline__ void circle_pair(int r, int k, int NP, int* p, int* q
   }
 }
 
-// A (p×p symmetric, FP64 in global) → lam (p, sorted by |λ| descending), W (p×p
-// eigenvectors as columns, same order).  Wtmp: p×p scratch for the unsorted
-// vectors.  Sweeps until no rotation is needed (or max_sweeps; *nsweeps out).
+// A (p×p symmetric, FP64 in global) → lam (p, sorted by |λ| descending, or by λ
+// descending when by_value), W (p×p eigenvectors as columns, same order).
+// Z: p×p scratch for the unsorted vectors.  Sweeps until no rotation is needed
+// (or max_sweeps; the sweep count goes to info[0]).
 template <typename T>
 __global__ void k_eigh_jacobi(const double* __restrict__ A, int p, int max_sweeps, double* __restrict__ lam,
-                              double* __restrict__ W, T* __restrict__ Z, int* __restrict__ info) {
+                              double* __restrict__ W, T* __restrict__ Z, int* __restrict__ info, int by_value) {
   extern __shared__ unsigned char smraw[];
   T* H = reinterpret_cast<T*>(smraw);  // p×p, leading dimension ld = p+1 (bank-conflict free)
   const int ld = p + 1;
@@ -250,13 +251,16 @@ __global__ void k_eigh_jacobi(const double* __restrict__ A, int p, int max_sweep
     __syncthreads();
     if (done) break;
   }
-  // sort by |λ| descending (ties by index): rank_j = #{i: |λ_i| > |λ_j| or (= and i<j)}
+  // sort by key descending (ties by index): rank_j = #{i: k_i > k_j or (= and i<j)},
+  // key |λ|, or λ itself when by_value
   for (int j = threadIdx.x; j < p; j += blockDim.x) {
     const double lj = (double)H[j + j * ld];
+    const double kj = by_value ? lj : fabs(lj);
     int rk = 0;
     for (int i = 0; i < p; ++i) {
       const double li = (double)H[i + i * ld];
-      rk += (fabs(li) > fabs(lj) || (fabs(li) == fabs(lj) && i < j)) ? 1 : 0;
+      const double ki = by_value ? li : fabs(li);
+      rk += (ki > kj || (ki == kj && i < j)) ? 1 : 0;
     }
     lam[rk] = lj;
     for (int i = 0; i < p; ++i) W[i + (int64_t)rk * p] = (double)Z[i + (int64_t)j * p];
@@ -265,7 +269,7 @@ __global__ void k_eigh_jacobi(const double* __restrict__ A, int p, int max_sweep
 }
 
 void eigh_small_prec(tnad_ctx* c, bool fp32, const double* A, int64_t p, double* W, double* lam, int max_sweeps,
-                     int* dev_info) {
+                     int* dev_info, bool by_value) {
   TNAD_REQUIRE(p >= 1 && p <= 256, TNAD_ERR_SHAPE, "eigh_small: p must be in [1,256]");
   WsScope scope(c);
   const size_t sm = (size_t)(p + 1) * p * (fp32 ? 4 : 8);
@@ -280,14 +284,14 @@ void eigh_small_prec(tnad_ctx* c, bool fp32, const double* A, int64_t p, double*
       attr32 = true;
     }
     float* Z = ws_f(c, p * p);
-    k_eigh_jacobi<float><<<1, 512, sm, c->stream>>>(A, (int)p, max_sweeps, lam, W, Z, dev_info);
+    k_eigh_jacobi<float><<<1, 512, sm, c->stream>>>(A, (int)p, max_sweeps, lam, W, Z, dev_info, by_value ? 1 : 0);
   } else {
     if (!attr64) {
       TNAD_CK(cudaFuncSetAttribute(k_eigh_jacobi<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSm));
       attr64 = true;
     }
     double* Z = ws_d(c, p * p);
-    k_eigh_jacobi<double><<<1, 512, sm, c->stream>>>(A, (int)p, max_sweeps, lam, W, Z, dev_info);
+    k_eigh_jacobi<double><<<1, 512, sm, c->stream>>>(A, (int)p, max_sweeps, lam, W, Z, dev_info, by_value ? 1 : 0);
   }
   count_launch(c);
   check_launch(c, "eigh_small");

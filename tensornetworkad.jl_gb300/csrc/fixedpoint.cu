@@ -14,6 +14,15 @@
 // uses z = U[:, 1:χ]·O with O = polar(U[:, 1:χ]ᵀ·z*), z* the projector that
 // produced x*, so that f(x*) = x* in the gauge of x*.  The pullback of the
 // polar alignment is included (ctmrg_step_bwd with O and zref).
+//
+// Where that alignment does not lock the gauge (the converged iteration keeps
+// moving x* by an orthogonal gauge transformation G on the χ index, e.g. a
+// period-2 cycle x* → G·x*·Gᵀ → x*, which the energy does not see), the map
+// whose fixed point x* is becomes g = Γ∘f: Γ(y) = Rᵀ·y·R rotates the step's
+// output back into x*'s gauge, with R = W·W*ᵀ, W and W* the eigenvectors of
+// C_y and C* ordered by λ and the columns of W signed so that y's T matches
+// T* in that basis.  Γ(G·x*·Gᵀ) = x* exactly, and Γ∘f no longer has the
+// gauge mode, so (I − (∂g/∂x)ᵀ)λ = x̄ is well posed again.
 #include <cmath>
 #include <vector>
 
@@ -29,6 +38,95 @@ void ns_polish_f64(tnad_ctx* c, double* O, int64_t m, int iters);
 
 namespace {
 
+// A_ij = F_ij·K_ij (i ≠ j), A_ii = Σ_k W*_ki·Y_ki: the eigenvector and
+// eigenvalue cotangents of C_y in its eigenbasis (F_ij = 1/(λ_j − λ_i)).
+__global__ void k_regauge_mid(const double* __restrict__ K, const double* __restrict__ F,
+                              const double* __restrict__ Wr, const double* __restrict__ Y, int chi,
+                              double* __restrict__ A) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (int64_t)chi * chi) return;
+  const int i = (int)(e % chi), j = (int)(e / chi);
+  if (i != j) {
+    A[e] = F[e] * K[e];
+  } else {
+    double t = 0.0;
+    for (int k = 0; k < chi; ++k) t += Wr[k + (int64_t)i * chi] * Y[k + (int64_t)i * chi];
+    A[e] = t;
+  }
+}
+
+// Γ of the header at y = (C_y, T_y): everything its pullback needs.
+struct Regauge {
+  int chi = 0, d = 0;
+  double *W = nullptr, *Wr = nullptr, *R = nullptr, *F = nullptr, *P = nullptr, *Q = nullptr;
+  double *X1, *Rb, *Wb, *K, *Y, *A, *Z;  // scratch of one pullback
+  // (C̄_y, T̄_y) = pullback of Γ at y for (C̄, T̄) = (dC, dT); outputs must not alias inputs.
+  void bwd(tnad_ctx* c, const double* dC, const double* dT, double* dCy, double* dTy) const {
+    const int64_t cd = (int64_t)chi * d;
+    // T̄_y = R·T̄·Rᵀ on the two χ legs
+    gemm_f64(c, 'N', 'N', chi, cd, chi, 1.0, R, chi, dT, chi, 0.0, X1, chi);
+    gemm_f64(c, 'N', 'T', cd, chi, chi, 1.0, X1, cd, R, chi, 0.0, dTy, cd);
+    // R̄ = (T_y ×₃ R)·T̄ᵀ (first leg) + (Rᵀ ×₁ T_y)ᵀ·T̄ (last leg)
+    gemm_f64(c, 'N', 'T', chi, chi, cd, 1.0, P, chi, dT, chi, 0.0, Rb, chi);
+    gemm_f64(c, 'T', 'N', chi, chi, cd, 1.0, Q, cd, dT, cd, 1.0, Rb, chi);
+    // W̄ = R̄·W*, K = Wᵀ·W̄, Y = C̄·W*  (C̃ = W*·diag(λ)·W*ᵀ gives λ̄ = diag(W*ᵀ·C̄·W*))
+    gemm_f64(c, 'N', 'N', chi, chi, chi, 1.0, Rb, chi, Wr, chi, 0.0, Wb, chi);
+    gemm_f64(c, 'T', 'N', chi, chi, chi, 1.0, W, chi, Wb, chi, 0.0, K, chi);
+    gemm_f64(c, 'N', 'N', chi, chi, chi, 1.0, dC, chi, Wr, chi, 0.0, Y, chi);
+    k_regauge_mid<<<(int)(((int64_t)chi * chi + 255) / 256), 256, 0, c->stream>>>(K, F, Wr, Y, chi, A);
+    count_launch(c);
+    check_launch(c, "regauge_mid");
+    // C̄_y = W·A·Wᵀ (its antisymmetric part is dropped by the step pullback's C + Cᵀ)
+    gemm_f64(c, 'N', 'N', chi, chi, chi, 1.0, W, chi, A, chi, 0.0, Z, chi);
+    gemm_f64(c, 'N', 'T', chi, chi, chi, 1.0, Z, chi, W, chi, 0.0, dCy, chi);
+  }
+};
+
+// Column signs s of W (eigenvectors of C_y) so that s_a·s_b·T̂_y(a,:,b) matches
+// T̂*(a,:,b) (both in their eigenbases): a spanning tree from the largest |λ*|,
+// each index joined through the already signed index it couples to most.
+// Returns the relative residuals of Γ(y) against x* in *rC, *rT.
+std::vector<double> regauge_signs(const std::vector<double>& ly, const std::vector<double>& lr,
+                                  const std::vector<double>& Thy, const std::vector<double>& Thr, int chi, int d,
+                                  double* rC, double* rT) {
+  const int64_t cd = (int64_t)chi * d;
+  auto at = [&](const std::vector<double>& X, int a, int i, int b) { return X[a + (int64_t)i * chi + b * cd]; };
+  std::vector<double> cab((size_t)chi * chi, 0.0);
+  for (int b = 0; b < chi; ++b)
+    for (int i = 0; i < d; ++i)
+      for (int a = 0; a < chi; ++a) cab[a + (size_t)b * chi] += at(Thy, a, i, b) * at(Thr, a, i, b);
+  std::vector<int> order(chi);
+  for (int a = 0; a < chi; ++a) order[a] = a;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return std::fabs(lr[x]) > std::fabs(lr[y]); });
+  std::vector<double> s(chi, 0.0);
+  std::vector<int> done;
+  s[order[0]] = 1.0;
+  done.push_back(order[0]);
+  for (int k = 1; k < chi; ++k) {
+    const int a = order[k];
+    int best = done[0];
+    for (int b : done)
+      if (std::fabs(cab[a + (size_t)b * chi]) > std::fabs(cab[a + (size_t)best * chi])) best = b;
+    s[a] = s[best] * (cab[a + (size_t)best * chi] < 0.0 ? -1.0 : 1.0);
+    done.push_back(a);
+  }
+  double nc = 0.0, dc = 0.0, nt = 0.0, dt = 0.0;
+  for (int a = 0; a < chi; ++a) {
+    nc += lr[a] * lr[a];
+    dc += (ly[a] - lr[a]) * (ly[a] - lr[a]);
+  }
+  for (int b = 0; b < chi; ++b)
+    for (int i = 0; i < d; ++i)
+      for (int a = 0; a < chi; ++a) {
+        const double r = at(Thr, a, i, b), y = s[a] * s[b] * at(Thy, a, i, b);
+        nt += r * r;
+        dt += (y - r) * (y - r);
+      }
+  *rC = nc > 0.0 ? std::sqrt(dc / nc) : 0.0;
+  *rT = nt > 0.0 ? std::sqrt(dt / nt) : 0.0;
+  return s;
+}
+
 struct Op {
   tnad_ctx* c;
   int prec;
@@ -39,15 +137,25 @@ struct Op {
   double* scratch_a;
   int64_t nCh, nx;
   double tsign;   // +1, or −1 when the step maps T* to −T* (see below)
-  double* sv;     // scratch for S·v
-  // w = v − (∂g/∂x)ᵀ v with g = S·f, S = diag(1 on C, tsign on T)
-  void apply(const double* v, double* w, double* jt) const {
+  double* sv;     // scratch for S·Γ̄(v)
+  const Regauge* rg;  // Γ, or null when f itself has x* as its fixed point
+  // u = (∂(Γ∘S)/∂y)ᵀ v: the cotangent of the step's output
+  const double* out_cotangent(const double* v) const {
     const double* u = v;
+    if (rg) {
+      rg->bwd(c, v, v + nCh, sv, sv + nCh);
+      u = sv;
+    }
     if (tsign < 0.0) {
-      copy_d2d(c, sv, v, nx);
+      if (u != sv) copy_d2d(c, sv, v, nx);
       scale(c, nx - nCh, -1.0, sv + nCh);
       u = sv;
     }
+    return u;
+  }
+  // w = v − (∂g/∂x)ᵀ v with g = Γ∘S·f, S = diag(1 on C, tsign on T)
+  void apply(const double* v, double* w, double* jt) const {
+    const double* u = out_cotangent(v);
     ctmrg_step_bwd(c, prec, a, d, chi, Cs, Ts, U, S, V, u, u + nCh, scratch_a, jt, jt + nCh, false, O, zref, cache);
     copy_d2d(c, w, v, nx);
     axpby(c, nx, -1.0, jt, 1.0, w);
@@ -209,7 +317,96 @@ FixedPointInfo ctmrg_fixedpoint_adjoint(tnad_ctx* c, int prec, const double* a_,
       std::fprintf(stderr, "[tnad trace] fixed point x*: |f_C - C|/|C| = %.3e  |f_T - T|/|T| = %.3e  |f_T + T|/|T| = %.3e\n",
                    r_c, r_plus, r_minus);
   }
+  // Γ (header): taken when it makes x* a fixed point to well below f's residual
+  Regauge rg;
+  bool use_rg = false;
+  if (info.fixed_point_residual > 1e-10 && chi <= 256) {
+    tr.mark("regauge");
+    const int64_t cd = (int64_t)chi * d;
+    rg.chi = chi;
+    rg.d = d;
+    rg.W = ws_d(c, nCh);
+    rg.Wr = ws_d(c, nCh);
+    rg.R = ws_d(c, nCh);
+    rg.F = ws_d(c, nCh);
+    rg.P = ws_d(c, nTe);
+    rg.Q = ws_d(c, nTe);
+    rg.X1 = ws_d(c, nTe);
+    rg.Rb = ws_d(c, nCh);
+    rg.Wb = ws_d(c, nCh);
+    rg.K = ws_d(c, nCh);
+    rg.Y = ws_d(c, nCh);
+    rg.A = ws_d(c, nCh);
+    rg.Z = ws_d(c, nCh);
+    double* Ty = ws_d(c, nTe);  // T of the step's output (sign applied below)
+    std::vector<double> ly(chi), lr(chi), Thy(nTe), Thr(nTe), Wh(nCh);
+    {
+      WsScope s1(c);
+      double* lam = ws_d(c, chi);
+      double* X = ws_d(c, nTe);
+      double* Th = ws_d(c, nTe);
+      // x*: λ*, W*, T̂* = W*ᵀ·T*·W*
+      eigh_small_prec(c, false, Cs, chi, rg.Wr, lam, 60, nullptr, true);
+      TNAD_CK(cudaMemcpyAsync(lr.data(), lam, chi * 8, cudaMemcpyDeviceToHost, c->stream));
+      gemm_f64(c, 'T', 'N', chi, cd, chi, 1.0, rg.Wr, chi, Ts, chi, 0.0, X, chi);
+      gemm_f64(c, 'N', 'N', cd, chi, chi, 1.0, X, cd, rg.Wr, chi, 0.0, Th, cd);
+      TNAD_CK(cudaMemcpyAsync(Thr.data(), Th, nTe * 8, cudaMemcpyDeviceToHost, c->stream));
+      TNAD_CK(cudaStreamSynchronize(c->stream));
+      // y = f(x*): λ_y, W (unsigned), T̂_y
+      eigh_small_prec(c, false, cache64.Cout, chi, rg.W, lam, 60, nullptr, true);
+      TNAD_CK(cudaMemcpyAsync(ly.data(), lam, chi * 8, cudaMemcpyDeviceToHost, c->stream));
+      gemm_f64(c, 'T', 'N', chi, cd, chi, 1.0, rg.W, chi, cache64.Tout, chi, 0.0, X, chi);
+      gemm_f64(c, 'N', 'N', cd, chi, chi, 1.0, X, cd, rg.W, chi, 0.0, Th, cd);
+      TNAD_CK(cudaMemcpyAsync(Thy.data(), Th, nTe * 8, cudaMemcpyDeviceToHost, c->stream));
+      TNAD_CK(cudaMemcpyAsync(Wh.data(), rg.W, nCh * 8, cudaMemcpyDeviceToHost, c->stream));
+      TNAD_CK(cudaStreamSynchronize(c->stream));
+    }
+    // both signs of T_y: T → −T maps T̂_y → −T̂_y
+    double best = info.fixed_point_residual, best_sign = tsign;
+    std::vector<double> best_s;
+    for (double sg : {1.0, -1.0}) {
+      std::vector<double> Ths(Thy);
+      if (sg < 0.0)
+        for (double& v : Ths) v = -v;
+      double rC = 0.0, rT = 0.0;
+      std::vector<double> sc = regauge_signs(ly, lr, Ths, Thr, chi, d, &rC, &rT);
+      const double r = std::max(rC, rT);
+      if (tr.on())
+        std::fprintf(stderr, "[tnad trace] re-gauged fixed point (T sign %+.0f): |C|-rel %.3e  |T|-rel %.3e\n", sg, rC,
+                     rT);
+      if (std::isfinite(r) && r < 0.1 * best) {
+        best = r;
+        best_sign = sg;
+        best_s = sc;
+      }
+    }
+    if (!best_s.empty()) {
+      use_rg = true;
+      tsign = best_sign;
+      info.fixed_point_residual = best;
+      // W ← W·diag(s); F_ij = 1/(λ_j − λ_i) (0 on the diagonal and at exact ties)
+      std::vector<double> Fh(nCh, 0.0);
+      for (int j = 0; j < chi; ++j) {
+        for (int i = 0; i < chi; ++i) {
+          Wh[i + (size_t)j * chi] *= best_s[j];
+          const double g = ly[j] - ly[i];
+          if (i != j && g != 0.0) Fh[i + (size_t)j * chi] = 1.0 / g;
+        }
+      }
+      TNAD_CK(cudaMemcpyAsync(rg.W, Wh.data(), nCh * 8, cudaMemcpyHostToDevice, c->stream));
+      TNAD_CK(cudaMemcpyAsync(rg.F, Fh.data(), nCh * 8, cudaMemcpyHostToDevice, c->stream));
+      copy_d2d(c, Ty, cache64.Tout, nTe);
+      if (tsign < 0.0) scale(c, nTe, -1.0, Ty);
+      // R = W·W*ᵀ, P = T_y ×₃ R ((χd)×χ), Q = Rᵀ ×₁ T_y (χ×(dχ))
+      gemm_f64(c, 'N', 'T', chi, chi, chi, 1.0, rg.W, chi, rg.Wr, chi, 0.0, rg.R, chi);
+      gemm_f64(c, 'N', 'N', cd, chi, chi, 1.0, Ty, cd, rg.R, chi, 0.0, rg.P, cd);
+      gemm_f64(c, 'T', 'N', chi, cd, chi, 1.0, rg.R, chi, Ty, chi, 0.0, rg.Q, chi);
+      TNAD_CK(cudaStreamSynchronize(c->stream));  // host vectors go out of scope
+    }
+  }
   info.tsign = tsign;
+  info.regauged = use_rg;
+  const Regauge* rgp = use_rg ? &rg : nullptr;
   if (prec != TNAD_PREC_FP64) {
     // GMRES with iterative refinement: the tensor-core operator solves for the
     // correction (to 1e-3, well above its ~1e-5 noise floor; 1e-4 cost more
@@ -219,8 +416,8 @@ FixedPointInfo ctmrg_fixedpoint_adjoint(tnad_ctx* c, int prec, const double* a_,
     WsScope s3(c);
     StepCache cache_tc;
     step_cache_fill(c, prec, a_, d, chi, Cs, Ts, U, O, cache_tc);
-    Op Atc{c, prec, a_, d, chi, Cs, Ts, U, S, V, O, zref, &cache_tc, scratch_a, nCh, nx, tsign, sv};
-    Op A64{c, TNAD_PREC_FP64, a_, d, chi, Cs, Ts, U, S, V, O, zref, &cache64, scratch_a, nCh, nx, tsign, sv};
+    Op Atc{c, prec, a_, d, chi, Cs, Ts, U, S, V, O, zref, &cache_tc, scratch_a, nCh, nx, tsign, sv, rgp};
+    Op A64{c, TNAD_PREC_FP64, a_, d, chi, Cs, Ts, U, S, V, O, zref, &cache64, scratch_a, nCh, nx, tsign, sv, rgp};
     info.iters += gmres(c, Atc, g, lam, m, std::max(tol, 1e-3), std::min(maxit, 40), &rel);
     tr.mark("refine");
     double* r = ws_d(c, nx);
@@ -247,15 +444,17 @@ FixedPointInfo ctmrg_fixedpoint_adjoint(tnad_ctx* c, int prec, const double* a_,
     // FP64 GMRES from the current λ to the requested tolerance
     tr.mark("gmres_f64");
     WsScope s3(c);
-    Op A{c, TNAD_PREC_FP64, a_, d, chi, Cs, Ts, U, S, V, O, zref, &cache64, scratch_a, nCh, nx, tsign, sv};
+    Op A{c, TNAD_PREC_FP64, a_, d, chi, Cs, Ts, U, S, V, O, zref, &cache64, scratch_a, nCh, nx, tsign, sv, rgp};
     info.iters += gmres(c, A, g, lam, m, tol, maxit, &rel);
   }
   info.residual = rel;
-  // ā += (∂g/∂a)ᵀ λ = (∂f/∂a)ᵀ S·λ
+  // ā += (∂g/∂a)ᵀ λ = (∂f/∂a)ᵀ S·Γ̄(λ)
   tr.mark("pullback_a");
   double* jt = ws_d(c, nx);
-  if (tsign < 0.0) scale(c, nx - nCh, -1.0, lam + nCh);
-  ctmrg_step_bwd(c, TNAD_PREC_FP64, a_, d, chi, Cs, Ts, U, S, V, lam, lam + nCh, dbulk, jt, jt + nCh, true, O, zref);
+  Op A{c, TNAD_PREC_FP64, a_, d, chi, Cs, Ts, U, S, V, O, zref, &cache64, scratch_a, nCh, nx, tsign, sv, rgp};
+  const double* u = A.out_cotangent(lam);
+  ctmrg_step_bwd(c, TNAD_PREC_FP64, a_, d, chi, Cs, Ts, U, S, V, u, u + nCh, dbulk, jt, jt + nCh, true, O, zref,
+                 &cache64);
   return info;
 }
 

@@ -210,6 +210,11 @@ void svd_jacobi(tnad_ctx* c, const double* A, int64_t m, int64_t n, double* U, d
 // Symmetric eigendecomposition of a small p×p matrix (p ≤ 256) by cyclic Jacobi in
 // one CTA: A = W·diag(lam)·Wᵀ, sorted by |lam| descending.
 void eigh_small(tnad_ctx* c, const double* A, int64_t p, double* W, double* lam);
+// The same with the sweep precision (fp32: FP32 rotations, FP64 in/out), a sweep
+// cap, the sweep count in dev_info[0] (may be null), and the order: |λ|
+// descending, or λ descending when by_value.
+void eigh_small_prec(tnad_ctx* c, bool fp32, const double* A, int64_t p, double* W, double* lam, int max_sweeps,
+                     int* dev_info, bool by_value = false);
 
 // ---------------- SVD adjoint (svd_back.cu) ----------------
 // Square thin SVD (n×n) with dU non-zero only in its first k columns (dUk n×k).

@@ -31,7 +31,8 @@ struct FixedPointInfo {
   int iters = 0;
   double residual = 0.0;
   double tsign = 1.0;  // −1: the converged T flips sign every step
-  double fixed_point_residual = 0.0;  // ‖g(x*) − x*‖/‖x*‖ of the aligned step at x*
+  double fixed_point_residual = 0.0;  // ‖g(x*) − x*‖/‖x*‖ of the map the adjoint differentiates
+  bool regauged = false;              // g includes the re-gauge of the step's output
 };
 
 // Implicit adjoint at a converged environment (C*, T*) of bulk a: given the

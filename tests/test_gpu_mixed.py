@@ -42,6 +42,32 @@ def test_mixed_energy_and_fixedpoint_gradient_D3_chi36(tn, orc):
     assert st["fixed_point_residual"] < 1e-6, st
 
 
+def test_mixed_gradient_D4_chi32_matches_difference_quotient(tn):
+    """D=4 N(0,1) site tensor, χ=32: the converged iteration cycles between
+    gauge-equivalent environments (x* → G·x*·Gᵀ → x*), which the energy does not
+    see.  The adjoint differentiates the step followed by the re-gauge onto x*,
+    whose fixed point x* is; its gradient matches a central difference of the
+    plain FP64 energy along a random direction and on one component."""
+    h = tn.hamiltonian(tn.Heisenberg())
+    A = tn.site_tensor("normal_maxabs", 4, 2, 0)
+    st = {}
+    _, g = tn.energy_and_gradient(h, tn.SquareIPEPS(A), 32, 1e-9, 400, opts=tn.mixed_opts(), stats=st)
+    assert st["fixed_point_residual"] < 1e-6, st
+    plain = tn.default_opts()
+    rng = np.random.default_rng(1)
+    d = rng.standard_normal(A.shape)
+    d /= np.linalg.norm(d)
+    e = np.zeros(A.shape)
+    e[1, 0, 1, 1, 1] = 1.0
+    for v, step in ((d, 1e-4), (e, 1e-5)):
+        Ep = tn.energy(h, tn.SquareIPEPS(np.asfortranarray(A + step * v)), 32, 1e-11, 400, plain)
+        Em = tn.energy(h, tn.SquareIPEPS(np.asfortranarray(A - step * v)), 32, 1e-11, 400, plain)
+        fd = (Ep - Em) / (2 * step)
+        gv = float(np.sum(g * v))
+        # difference-quotient error: O(step²) plus ~1e-12/step from the stop rule
+        assert abs(gv - fd) <= 1e-4 * abs(fd) + 2e-7, (gv, fd, st)
+
+
 def test_plain_fixedpoint_adjoint_matches_unrolled(tn, orc):
     h = tn.hamiltonian(tn.Heisenberg())
     A = orc.ipeps_uniform(2, 2, 7)

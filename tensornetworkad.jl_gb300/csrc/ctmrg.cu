@@ -252,7 +252,10 @@ void ctmrg_step_bwd(tnad_ctx* c, int prec, const double* a_, int d, int chi, con
     // z = U_χ·O(U_χ) with O = polar(U_χᵀ·R), R = zref held fixed.  Pullback of
     // the polar factor at X ≈ O:  Ū_χ = (z̄ − R·skew(zᵀ·z̄))·Oᵀ, which makes
     // U_χᵀ·Ū_χ symmetric: rotations inside the kept subspace (pure gauge) carry
-    // no cotangent, so their 1/(λ_i − λ_j) factors in svd_back never act.
+    // no cotangent, so their 1/(λ_i − λ_j) factors in svd_back never act.  The
+    // kept block of svd_back is skipped outright: M's spectrum can come in ±θ
+    // pairs (degenerate singular values), and the rounding left in the
+    // antisymmetric part (TF32X3 products) times their F_ij is not small.
     double* B = ws_d(c, (int64_t)chi * chi);
     double* Sk = ws_d(c, (int64_t)chi * chi);
     double* dz2 = ws_d(c, n * chi);
@@ -267,7 +270,7 @@ void ctmrg_step_bwd(tnad_ctx* c, int prec, const double* a_, int d, int chi, con
   }
   double* dM = ws_d(c, n * n);
   // svd_back(U, S, V, [dU_χ 0], nothing, nothing) with the χ-column structure exploited
-  svd_back_cols(c, prec, U, S, V, n, chi, dUfull, 1e-40, dM);
+  svd_back_cols(c, prec, U, S, V, n, chi, dUfull, 1e-40, dM, O != nullptr);
   // cpmat += cpmat'  →  dcp += dM + dMᵀ
   double* dMs = ws_d(c, n * n);
   add_transpose(c, n, dM, dMs);

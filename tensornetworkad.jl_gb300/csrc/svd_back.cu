@@ -38,8 +38,11 @@ __global__ void k_scale_cols(int64_t m, int64_t n, double* __restrict__ P, const
 // dS = dV = nothing): with Xk = Uᵀ·dU[:, 1:k],
 //   R1[i,j] = F_ij·(Xk[i,j] − [i<k]·Xk[j,i])·s_j      (all i, j < k)
 //   R2[i,j] = −F_ij·Xk[j,i]·s_j                       (i < k, j ≥ k; stored at j−k)
+// kept_sym: the caller's dU makes the kept block Xk[1:k, 1:k] symmetric, so
+// R1's kept block is exactly 0 and is set so (rounding in its antisymmetric part
+// would otherwise be multiplied by F_ij of (near-)degenerate kept pairs).
 __global__ void k_svdback_cols(int64_t n, int64_t k, const double* __restrict__ S, const double* __restrict__ Xk,
-                               double eta, double* __restrict__ R1, double* __restrict__ R2) {
+                               double eta, int kept_sym, double* __restrict__ R1, double* __restrict__ R2) {
   const int64_t n1 = n * k, n2 = k * (n - k);
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n1 + n2; e += (int64_t)gridDim.x * blockDim.x) {
     int64_t i, j;
@@ -55,6 +58,10 @@ __global__ void k_svdback_cols(int64_t n, int64_t k, const double* __restrict__ 
     const double d = __dsub_rn(__dmul_rn(sj, sj), __dmul_rn(si, si));
     const double fij = __ddiv_rn(d, __dadd_rn(__dmul_rn(d, d), eta));
     if (e < n1) {
+      if (kept_sym && i < k) {
+        R1[e] = 0.0;
+        continue;
+      }
       const double xij = Xk[i + j * n];
       const double xji = i < k ? Xk[j + i * n] : 0.0;
       R1[e] = __dmul_rn(__dadd_rn(__dmul_rn(fij, xij), __dmul_rn(-fij, xji)), sj);
@@ -66,14 +73,14 @@ __global__ void k_svdback_cols(int64_t n, int64_t k, const double* __restrict__ 
 
 // svd_back for a square thin SVD with dU = [dUk, 0] (k leading columns), dS = dV = nothing.
 void svd_back_cols(tnad_ctx* c, int prec, const double* U, const double* S, const double* V, int64_t n, int64_t k,
-                   const double* dUk, double eta, double* dA) {
+                   const double* dUk, double eta, double* dA, bool kept_sym) {
   WsScope scope(c);
   double* Xk = ws_d(c, n * k);
   gemm(c, prec, 'T', 'N', n, k, n, 1.0, U, n, dUk, n, 0.0, Xk, n);
   double* R1 = ws_d(c, n * k);
   double* R2 = ws_d(c, k * (n - k) + 1);
   const int64_t tot = n * k + k * (n - k);
-  k_svdback_cols<<<(int)std::min<int64_t>((tot + 255) / 256, 4096), 256, 0, c->stream>>>(n, k, S, Xk, eta, R1, R2);
+  k_svdback_cols<<<(int)std::min<int64_t>((tot + 255) / 256, 4096), 256, 0, c->stream>>>(n, k, S, Xk, eta, kept_sym ? 1 : 0, R1, R2);
   count_launch(c);
   check_launch(c, "svdback_cols");
   // dA = (U·R1)·V[:, 1:k]ᵀ + U[:, 1:k]·(R2·V[:, k+1:n]ᵀ)

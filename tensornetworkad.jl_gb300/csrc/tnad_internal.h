@@ -218,8 +218,10 @@ void eigh_small_prec(tnad_ctx* c, bool fp32, const double* A, int64_t p, double*
 
 // ---------------- SVD adjoint (svd_back.cu) ----------------
 // Square thin SVD (n×n) with dU non-zero only in its first k columns (dUk n×k).
+// kept_sym: Uᵀ·dU is symmetric on the kept k×k block (a gauge-invariant use of
+// U[:, 1:k]), whose terms are then exactly 0 and skipped.
 void svd_back_cols(tnad_ctx* c, int prec, const double* U, const double* S, const double* V, int64_t n, int64_t k,
-                   const double* dUk, double eta, double* dA);
+                   const double* dUk, double eta, double* dA, bool kept_sym = false);
 // svd_back for thin SVD (U m×n, S n, V n×n), dU m×n or null, dS n or null, dV n×n or null.
 void svd_back(tnad_ctx* c, int prec, const double* U, const double* S, const double* V, int64_t m,
               int64_t n, const double* dU, const double* dS, const double* dV, double eta,

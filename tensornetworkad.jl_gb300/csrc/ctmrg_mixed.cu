@@ -14,9 +14,11 @@
 // FP64 Jacobi) until ‖Δ(|θ|/|θ₁|)_{1:χ}‖₂ ≤ tol.  Any orthonormal basis of the
 // top-χ subspace gives a gauge-equivalent environment, so the fixed point is
 // the reference's.  The polar alignment keeps consecutive environments in one
-// gauge, which the implicit adjoint needs (x* = f(x*)); where the projector's
-// gauge near the χ cut keeps moving (D=4 workloads) that premise fails, and
-// tnad_energy_fixed_point_residual reports it.
+// gauge, which the implicit adjoint needs (x* = f(x*)).  Where C's spectrum
+// comes in ±λ pairs (D=4 workloads) the converged iteration still cycles
+// between gauge-equivalent environments; the adjoint then re-gauges the step's
+// output onto x* (fixedpoint.cu), and tnad_energy_fixed_point_residual reports
+// the residual of the map it differentiates.
 #include <cmath>
 #include <cstdio>
 #include <limits>

@@ -290,10 +290,9 @@ FixedPointInfo ctmrg_fixedpoint_adjoint(tnad_ctx* c, int prec, const double* a_,
   // can sit on T* = −f_T(x*): C and the energy are converged but T flips sign
   // every step.  Then x* is a fixed point of g = S·f with S = −1 on T, and the
   // adjoint is taken for g.  The sign is only trusted when x* is a fixed point
-  // of g to ~1e-6 while it is not one of f.  (When neither holds — the aligned
-  // gauge has not locked, e.g. a truncation cut through a slowly decaying
-  // spectrum — the implicit adjoint's premise fails; the residuals are printed
-  // under TNAD_TRACE.)
+  // of g to ~1e-6 while it is not one of f.  When neither holds, the aligned
+  // gauge has not locked and the re-gauge Γ below is tried (with either sign of
+  // T); the residuals are printed under TNAD_TRACE.
   double* sv = ws_d(c, nx);
   StepCache cache64;  // FP64 forward intermediates of the step at x* (all FP64 operators share them)
   step_cache_fill(c, TNAD_PREC_FP64, a_, d, chi, Cs, Ts, U, O, cache64);

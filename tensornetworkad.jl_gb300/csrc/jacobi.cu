@@ -315,8 +315,13 @@ __global__ void k_rank(const double* __restrict__ s, int64_t n, int* __restrict_
 
 // Scatter sorted: S[rank j] = ‖W_j‖, V_out[:, rank j] = V_j and
 //  - symmetric A: U[:, rank j] = sign(V_j·W_j)·V_j — the left vectors of a
-//    symmetric matrix are its signed right vectors, and V (a product of plane
-//    rotations) is orthogonal to working precision, including null columns;
+//    symmetric matrix are its signed right vectors when V_j is an eigenvector,
+//    and V (a product of plane rotations) is orthogonal to working precision,
+//    including null columns.  A column whose singular value is shared (to
+//    1e-8 relative) with another one, e.g. a pair of eigenvalues ±λ, is only
+//    determined up to a rotation inside that singular subspace, and there V_j
+//    need not be an eigenvector: such a column (above the weak threshold) takes
+//    U[:, rank j] = W_j/‖W_j‖ = A·V_j/σ_j, so that U, S, V stay an SVD;
 //  - general A: U[:, rank j] = W_j/‖W_j‖; columns below weak_rel·‖A‖_F (whose
 //    direction carries the ε·‖A‖ rounding noise) are counted and afterwards
 //    re-orthonormalised against all larger ones by k_complete_col.
@@ -328,9 +333,15 @@ __global__ void k_scatter(const double* __restrict__ W, const double* __restrict
   int r = rank[j];
   double sj = s[j];
   bool weak = !(sj > weak_rel * sqrt(fro2[0])) || !(sj > 1e-300);
+  // shared singular value (symmetric A): does another column have σ within 1e-8·σ_j?
+  int shared = 0;
+  if (symmetric && !weak)
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x)
+      shared |= (i != j && fabs(s[i] - sj) <= 1e-8 * sj) ? 1 : 0;
+  shared = __syncthreads_or(shared);
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
     double u;
-    if (symmetric)
+    if (symmetric && !shared)
       u = i < n ? sg[j] * Vw[i + j * n] : 0.0;
     else
       u = sj > 1e-300 ? W[i + j * m] / sj : 0.0;

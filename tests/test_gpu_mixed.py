@@ -68,6 +68,24 @@ def test_mixed_gradient_D4_chi32_matches_difference_quotient(tn):
         assert abs(gv - fd) <= 1e-4 * abs(fd) + 2e-7, (gv, fd, st)
 
 
+def test_plain_gradient_D4_chi32_matches_difference_quotient(tn):
+    """The plain FP64 path (full symmetric Jacobi SVD each step, unrolled reverse:
+    the reference's semantics) on the same D=4 tensor.  M's spectrum comes in ±λ
+    pairs, so its singular values are pairwise degenerate; the decomposition must
+    still be an SVD (U = A·V/σ on those columns) for svd_back to hold."""
+    h = tn.hamiltonian(tn.Heisenberg())
+    A = tn.site_tensor("normal_maxabs", 4, 2, 0)
+    plain = tn.default_opts()
+    _, g = tn.energy_and_gradient(h, tn.SquareIPEPS(A), 32, 1e-9, 400, opts=plain)
+    idx, step = (1, 0, 1, 1, 1), 1e-5
+    p, m = A.copy(), A.copy()
+    p[idx] += step
+    m[idx] -= step
+    fd = (tn.energy(h, tn.SquareIPEPS(p), 32, 1e-11, 400, plain) -
+          tn.energy(h, tn.SquareIPEPS(m), 32, 1e-11, 400, plain)) / (2 * step)
+    assert abs(g[idx] - fd) <= 1e-4 * abs(fd) + 2e-7, (g[idx], fd)
+
+
 def test_plain_fixedpoint_adjoint_matches_unrolled(tn, orc):
     h = tn.hamiltonian(tn.Heisenberg())
     A = orc.ipeps_uniform(2, 2, 7)

@@ -84,6 +84,8 @@ def test_aligned_ctmrg_cycles_and_the_regauged_adjoint_is_the_energy_derivative(
         C, T, _ = ro.aligned_ctmrg(a, 16, 100)[-1]
         return float(o.expectationvalue(torch.as_tensor(h), ap, C, T))
 
+    # the aligned iteration converges to the reference CTMRG's energy (src/ctmrg.jl step)
+    assert abs(E - float(o.energy(h, torch.as_tensor(A), 16, 1e-12, 300))) < 1e-10
     v = np.random.default_rng(1).standard_normal(A.shape)
     v /= np.linalg.norm(v)
     step = 1e-4

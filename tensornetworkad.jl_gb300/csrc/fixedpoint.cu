@@ -341,21 +341,21 @@ FixedPointInfo ctmrg_fixedpoint_adjoint(tnad_ctx* c, int prec, const double* a_,
     std::vector<double> ly(chi), lr(chi), Thy(nTe), Thr(nTe), Wh(nCh);
     {
       WsScope s1(c);
-      double* lam = ws_d(c, chi);
-      double* X = ws_d(c, nTe);
+      double* ev = ws_d(c, chi);
+      double* WT = ws_d(c, nTe);
       double* Th = ws_d(c, nTe);
       // x*: λ*, W*, T̂* = W*ᵀ·T*·W*
-      eigh_small_prec(c, false, Cs, chi, rg.Wr, lam, 60, nullptr, true);
-      TNAD_CK(cudaMemcpyAsync(lr.data(), lam, chi * 8, cudaMemcpyDeviceToHost, c->stream));
-      gemm_f64(c, 'T', 'N', chi, cd, chi, 1.0, rg.Wr, chi, Ts, chi, 0.0, X, chi);
-      gemm_f64(c, 'N', 'N', cd, chi, chi, 1.0, X, cd, rg.Wr, chi, 0.0, Th, cd);
+      eigh_small_prec(c, false, Cs, chi, rg.Wr, ev, 60, nullptr, true);
+      TNAD_CK(cudaMemcpyAsync(lr.data(), ev, chi * 8, cudaMemcpyDeviceToHost, c->stream));
+      gemm_f64(c, 'T', 'N', chi, cd, chi, 1.0, rg.Wr, chi, Ts, chi, 0.0, WT, chi);
+      gemm_f64(c, 'N', 'N', cd, chi, chi, 1.0, WT, cd, rg.Wr, chi, 0.0, Th, cd);
       TNAD_CK(cudaMemcpyAsync(Thr.data(), Th, nTe * 8, cudaMemcpyDeviceToHost, c->stream));
       TNAD_CK(cudaStreamSynchronize(c->stream));
       // y = f(x*): λ_y, W (unsigned), T̂_y
-      eigh_small_prec(c, false, cache64.Cout, chi, rg.W, lam, 60, nullptr, true);
-      TNAD_CK(cudaMemcpyAsync(ly.data(), lam, chi * 8, cudaMemcpyDeviceToHost, c->stream));
-      gemm_f64(c, 'T', 'N', chi, cd, chi, 1.0, rg.W, chi, cache64.Tout, chi, 0.0, X, chi);
-      gemm_f64(c, 'N', 'N', cd, chi, chi, 1.0, X, cd, rg.W, chi, 0.0, Th, cd);
+      eigh_small_prec(c, false, cache64.Cout, chi, rg.W, ev, 60, nullptr, true);
+      TNAD_CK(cudaMemcpyAsync(ly.data(), ev, chi * 8, cudaMemcpyDeviceToHost, c->stream));
+      gemm_f64(c, 'T', 'N', chi, cd, chi, 1.0, rg.W, chi, cache64.Tout, chi, 0.0, WT, chi);
+      gemm_f64(c, 'N', 'N', cd, chi, chi, 1.0, WT, cd, rg.W, chi, 0.0, Th, cd);
       TNAD_CK(cudaMemcpyAsync(Thy.data(), Th, nTe * 8, cudaMemcpyDeviceToHost, c->stream));
       TNAD_CK(cudaMemcpyAsync(Wh.data(), rg.W, nCh * 8, cudaMemcpyDeviceToHost, c->stream));
       TNAD_CK(cudaStreamSynchronize(c->stream));
@@ -388,8 +388,8 @@ FixedPointInfo ctmrg_fixedpoint_adjoint(tnad_ctx* c, int prec, const double* a_,
       for (int j = 0; j < chi; ++j) {
         for (int i = 0; i < chi; ++i) {
           Wh[i + (size_t)j * chi] *= best_s[j];
-          const double g = ly[j] - ly[i];
-          if (i != j && g != 0.0) Fh[i + (size_t)j * chi] = 1.0 / g;
+          const double gap = ly[j] - ly[i];
+          if (i != j && gap != 0.0) Fh[i + (size_t)j * chi] = 1.0 / gap;
         }
       }
       TNAD_CK(cudaMemcpyAsync(rg.W, Wh.data(), nCh * 8, cudaMemcpyHostToDevice, c->stream));

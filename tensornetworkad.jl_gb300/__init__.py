@@ -427,18 +427,30 @@ def optimiseipeps(ipeps: IPEPS, h, chi: int, tol: float, maxit: int, f_tol: floa
     return float(r.fun), r.x.reshape(shape, order="F")
 
 
-def num_grad(f, K, delta: float = 1e-5):
-    """(f(K+δ/2) − f(K−δ/2))/δ, elementwise for arrays (src/autodiff.jl:44-63)."""
+def num_grad(f, K, delta: float = 1e-5, dist=None):
+    """(f(K+δ/2) − f(K−δ/2))/δ, elementwise for arrays (src/autodiff.jl:44-63).
+
+    dist: an initialised torch.distributed process group (one rank per GPU).
+    The elements are then independent units: each rank differentiates a
+    contiguous share of them and every rank returns the gathered array."""
     if np.isscalar(K):
         return (f(K + delta / 2) - f(K - delta / 2)) / delta
     K = np.asarray(K, dtype=np.float64)
-    g = np.zeros_like(K)
-    for i in np.ndindex(K.shape):
+    idx = list(np.ndindex(K.shape))
+    rank, world = 0, 1
+    if dist is not None and dist.is_initialized():
+        rank, world = dist.get_rank(), dist.get_world_size()
+    part = []
+    for i in idx[len(idx) * rank // world:len(idx) * (rank + 1) // world]:
         kp, km = K.copy(), K.copy()
         kp[i] += delta / 2
         km[i] -= delta / 2
-        g[i] = (f(kp) - f(km)) / delta
-    return g
+        part.append((f(kp) - f(km)) / delta)
+    if world > 1:
+        parts = [None] * world
+        dist.all_gather_object(parts, part)
+        part = [v for p in parts for v in p]
+    return np.asarray(part, dtype=np.float64).reshape(K.shape)
 
 
 def mag_tensor(model: Ising, beta: float) -> np.ndarray:

@@ -1,12 +1,14 @@
-"""Replica path on CPU: two gloo ranks exercise the host logic that bench.py
-and the warm-start data generation run with one process per GPU — the
-max-over-ranks step time, the barrier, the contiguous sharding of independent
-site tensors and the gather of every rank's share in rank order."""
+"""Replica path on CPU: two gloo ranks exercise the host logic that bench.py,
+the warm-start data generation and the difference-quotient gradient run with
+one process per GPU — the max-over-ranks step time, the barrier, the contiguous
+sharding of independent units (site tensors, gradient elements) and the gather
+of every rank's share in rank order."""
 import os
 import socket
 import sys
 from pathlib import Path
 
+import numpy as np
 import pytest
 
 ROOT = Path(__file__).resolve().parent.parent
@@ -34,7 +36,9 @@ def _rank(rank, world, port, q):
         t = bench.max_over_ranks(dist, 1.0 + 2.5 * r)
         mine = list(wl.shard_range(11, r, w))
         allv = wl.gather_shards([10 * i for i in mine], dist)
-        q.put((r, t, mine, allv))
+        K = np.arange(30, dtype=np.float64).reshape(2, 3, 5) / 7.0
+        g = tn.num_grad(lambda x: float(np.sum(x ** 3)), K, 1e-4, dist=dist)
+        q.put((r, t, mine, allv, g))
     finally:
         dist.destroy_process_group()
 
@@ -56,6 +60,9 @@ def test_two_gloo_ranks_max_time_shard_and_gather():
     assert [o[1] for o in out] == [3.5, 3.5]  # every rank sees the slowest rank's time
     assert out[0][2] + out[1][2] == list(range(11))  # contiguous, disjoint, complete
     assert out[0][3] == out[1][3] == [10 * i for i in range(11)]
+    K = np.arange(30, dtype=np.float64).reshape(2, 3, 5) / 7.0
+    for o in out:  # each rank differentiated half of the elements; both hold all of them
+        assert np.allclose(o[4], 3 * K ** 2, rtol=1e-8, atol=1e-8)
 
 
 def test_shard_range_covers_every_unit_once():

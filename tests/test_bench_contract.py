@@ -22,3 +22,38 @@ def test_reference_arm_prints_one_contract_line():
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1 and d["cpu_baseline"]["sample"]
     assert d["e2e"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
     assert d["config"]["workload"] == "heisenberg_D4_chi64"
+
+
+def test_gradient_check_compares_both_gradients_with_a_central_difference():
+    """bench.gradient_check on a quadratic energy (exact central difference),
+    with a stand-in for the package: the mixed gradient exact, the plain one off."""
+    import numpy as np
+
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    Q = np.diag(np.arange(1.0, 9.0))
+
+    class FakeTn:
+        @staticmethod
+        def default_opts():
+            return None
+
+        @staticmethod
+        def SquareIPEPS(A):
+            return A
+
+        @staticmethod
+        def energy(h, A, chi, tol, maxit, opts):
+            x = np.asarray(A).ravel()
+            return 0.5 * float(x @ Q @ x)
+
+    class FakeSol:
+        A = np.linspace(0.1, 0.8, 8).reshape(2, 2, 2)
+        h, chi, maxit = None, 4, 10
+
+    g_exact = (Q @ FakeSol.A.ravel()).reshape(2, 2, 2)
+    r = bench.gradient_check(FakeTn, FakeSol, g_exact, 1.01 * g_exact)
+    assert r["mixed_rel_err"] < 1e-9
+    assert abs(r["plain_unrolled_rel_err"] - 0.01) < 1e-8
+    assert abs(r["mixed_vs_plain_rel_l2"] - 0.01 / 1.01) < 1e-12

@@ -316,10 +316,12 @@ FixedPointInfo ctmrg_fixedpoint_adjoint(tnad_ctx* c, int prec, const double* a_,
       std::fprintf(stderr, "[tnad trace] fixed point x*: |f_C - C|/|C| = %.3e  |f_T - T|/|T| = %.3e  |f_T + T|/|T| = %.3e\n",
                    r_c, r_plus, r_minus);
   }
-  // Γ (header): taken when it makes x* a fixed point to well below f's residual
+  // Γ (header): taken when it makes x* a fixed point to well below f's residual.
+  // Its χ×χ eigenproblems run in one CTA's shared memory (FP64, ≤ 200 KB).
   Regauge rg;
   bool use_rg = false;
-  if (info.fixed_point_residual > 1e-10 && chi <= 256) {
+  const bool rg_fits = (int64_t)(chi + 1) * chi * 8 <= 200 * 1024;
+  if (info.fixed_point_residual > 1e-10 && rg_fits) {
     tr.mark("regauge");
     const int64_t cd = (int64_t)chi * d;
     rg.chi = chi;

@@ -9,7 +9,7 @@ the same seeded input (tests/golden/estar.json).
                     [--workload heisenberg_D4_chi64] [--mode mixed|plain]
 
 --impl reference times the CPU restatement of the reference (the oracle:
-torch-CPU FP64, all host threads) on a bounded sample of the same workload.
+torch-CPU FP64, all host threads), one full solve of the same workload per step.
 With N > 1 every rank solves its own replica (the CTMRG fixed point is
 sequential; there is no collective on the data path).
 """
@@ -32,6 +32,12 @@ sys.path.insert(0, str(ROOT))
 
 ESTAR = json.loads((ROOT / "tests" / "golden" / "estar.json").read_text())
 TARGET = 1e-8
+
+
+def metric_for(w) -> str:
+    """The metric string both arms print for workload w (identical by construction)."""
+    return (f"CTMRG energy+gradient time to |dE|<=1e-8 vs the FP64 oracle "
+            f"(Heisenberg iPEPS D={w['D']}, chi={w['chi']})")
 
 
 def parse():
@@ -153,8 +159,8 @@ def barrier(dist):
 PEAKS_PATH = ROOT / "MEASURED_PEAKS.json"
 FP64_NOMINAL_TFLOPS = 1.25  # GB300 FP64 (no measured FP64 figure exists for this machine)
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the FP64 Jacobi round
-# (16 805 888 + 0 bytes; ncu flushes the caches between its passes), from the
-# capture summarised in profiles/jacobi_round_D4_chi64.md
+# at n = 1024 (16 805 888 + 0 bytes; ncu flushes the caches between its passes),
+# from one ncu capture of that kernel on this workload
 JACOBI_ROUND_TRAFFIC_BYTES = 16805888
 
 
@@ -234,6 +240,14 @@ def kernel_timer_read(c):
     return n.value, ms.value, work.value
 
 
+def l2_flush(buf, stream):
+    """Overwrite a buffer larger than the 129 MB L2 on the library's stream."""
+    import torch
+
+    with torch.cuda.stream(stream):
+        buf.add_(1.0)
+
+
 def run_gb300(args):
     import torch
     import __graft_entry__ as ge
@@ -245,34 +259,38 @@ def run_gb300(args):
     w = ESTAR[args.workload]
     sol = Solver(tn, w, args.mode)
     c = sol.c
+    stream = torch.cuda.ExternalStream(c.lib.tnad_ctx_stream(c.h))
+    flush = torch.zeros(64 << 20, dtype=torch.float32, device="cuda")  # 256 MB > L2
     for _ in range(args.warmup):
         sol.device()
     torch.cuda.synchronize()
     barrier(dist)
-    # timed region: K solves with device-resident inputs (no kernel timer)
+    # timed region: K solves with device-resident inputs (no kernel timer); L2
+    # flushed between solves, outside each solve's pair of CUDA events
     l0 = c.launches
-    errs, stats = [], []
+    errs, stats, evs = [], [], []
     with Clocks(local) as clk:
         torch.cuda.synchronize()
         barrier(dist)
-        stream = torch.cuda.ExternalStream(c.lib.tnad_ctx_stream(c.h))
-        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        ev0.record(stream)
         for _ in range(args.steps):
+            l2_flush(flush, stream)
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
             E, st = sol.device()
+            ev1.record(stream)
+            evs.append((ev0, ev1))
             errs.append(abs(E - w["E_star"]))
             stats.append(st)
-        ev1.record(stream)
         torch.cuda.synchronize()
         barrier(dist)
     launches = (c.launches - l0) // args.steps
-    t_dev = max_over_ranks(dist, ev0.elapsed_time(ev1) / 1e3 / args.steps)
+    t_dev = max_over_ranks(dist, sum(e0.elapsed_time(e1) for e0, e1 in evs) / 1e3 / args.steps)
     # one extra solve per kernel family with its launches bracketed by CUDA
     # events on the library's stream (a Jacobi sweep replayed as a CUDA graph
     # is bracketed as a whole: its average launch duration includes the
     # graph's gaps between rounds)
     fam = {}
-    for name in ("jacobi_round", "jacobi_round_f32", "gemm_tf32x3"):
+    for name in ("jacobi_round", "jacobi_round_f32", "gemm_tf32x3", "gemm_f64"):
         kernel_timer(c, name)
         sol.device()
         fam[name] = kernel_timer_read(c)
@@ -280,45 +298,55 @@ def run_gb300(args):
     kn, kms, kwork = fam["jacobi_round"]
     tn_n, tn_ms, tn_work = fam["gemm_tf32x3"]
     k32n, k32ms, k32work = fam["jacobi_round_f32"]
-    # end to end through the public API with host (NumPy) arrays
+    gf_n, gf_ms, gf_work = fam["gemm_f64"]
+    # end to end through the public API with host (NumPy) arrays: every call
+    # copies A and h to the device and E and dE/dA back
     sol.host()
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     for _ in range(args.steps):
         E_h, g_h, st_h = sol.host()
     t_e2e = max_over_ranks(dist, (time.perf_counter() - t1) / args.steps)
-    # the plain FP64 GPU path (full Jacobi SVD each step, unrolled reverse), one solve
-    plain, grad_check = None, None
+    # the plain FP64 GPU path (full Jacobi SVD each step, unrolled reverse): one
+    # warm-up solve, then the mean of three timed ones
+    plain, grad_check, g_plain = None, None, None
     if args.mode == "mixed" and not args.no_plain:
         ps = Solver(tn, w, "plain")
-        t2 = time.perf_counter()
-        Ep, stp = ps.device()
-        torch.cuda.synchronize()
-        tp_ = time.perf_counter() - t2
-        plain = {"value": round(tp_, 4), "unit": "s", "ctmrg_steps": stp["steps"], "delta_E": abs(Ep - w["E_star"]),
-                 "steps": 1, "warmup": 0}
+        ps.device()
+        tps, eps_ = [], []
+        for _ in range(3):
+            torch.cuda.synchronize()
+            t2 = time.perf_counter()
+            Ep, stp = ps.device()
+            torch.cuda.synchronize()
+            tps.append(time.perf_counter() - t2)
+            eps_.append(abs(Ep - w["E_star"]))
+        plain = {"value": round(statistics.mean(tps), 4), "unit": "s", "ctmrg_steps": stp["steps"],
+                 "delta_E": max(eps_), "steps": 3, "warmup": 1, "min": round(min(tps), 4), "max": round(max(tps), 4)}
+        g_plain = ps.g_d.cpu().numpy().reshape(np.shape(sol.A), order="F")
         if rank == 0:
-            grad_check = gradient_check(tn, sol, g_h, ps.g_d.cpu().numpy().reshape(np.shape(sol.A), order="F"))
+            grad_check = gradient_check(tn, sol, g_h, g_plain)
     if rank != 0:
         return
     pk, pk_kind = peaks()
     rounds = kn
     ach_fp64 = (kwork / (kms / 1e3)) / 1e12 if kms > 0 else None
     ach_tc = (tn_work / (tn_ms / 1e3)) / 1e12 if tn_ms > 0 else None
+    ach_gf = (gf_work / (gf_ms / 1e3)) / 1e12 if gf_ms > 0 else None
     tf32_peak = pk.get("bf16_tflops", 1900.0) / 2.0
     nA = int(np.asarray(sol.A).size)
     line = {
-        "metric": "CTMRG energy+gradient time to |dE|<=1e-8 vs the FP64 oracle (Heisenberg iPEPS D=4, chi=64)",
+        "metric": metric_for(w),
         "value": round(t_dev, 6), "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(t_dev * 1e3, 3), "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.mode == "plain" else "tf32x3+f64",
-        "data": "synthetic: N(0,1) site tensor (NumPy seed 0), max-abs normalised, symmetrised",
+        "data": f"synthetic: {w['recipe']} site tensor (NumPy seed {w['seed']}), symmetrised",
         "config": {"workload": args.workload, "D": sol.D, "chi": sol.chi, "phys": sol.s, "mode": args.mode,
                    "stop_tol": sol.tol, "ctmrg_steps": stats[-1]["steps"], "fp64_steps": stats[-1]["fp64_steps"],
                    "fixedpoint_iters": stats[-1]["fp_iters"],
                    "fixedpoint_residual": stats[-1].get("fixed_point_residual"),
                    "parallelism": f"replicas x{world}",
-                   "l2": "no flush: each solve runs ~10^4 launches over a <300 MB working set (L2/HBM resident)"},
+                   "l2": "flushed between timed solves (256 MB write on the library stream, outside the events)"},
         "delta_E": max(errs), "E": E, "E_star": w["E_star"],
         "e2e": {"value": round(t_e2e, 6), "unit": "s", "h2d_bytes_per_step": 8 * (nA + 16),
                 "d2h_bytes_per_step": 8 * (nA + 1)},
@@ -342,45 +370,61 @@ def run_gb300(args):
                             "peak": tf32_peak, "unit": "TFLOP/s",
                             "frac": round(3 * ach_tc / tf32_peak, 4) if ach_tc else None,
                             "peak_kind": f"{pk_kind} bf16 burst / 2 (dense TF32 rate)",
-                            "launches_per_step": tn_n, "avg_launch_us": round(tn_ms * 1e3 / tn_n, 3) if tn_n else None},
+                            "launches_per_step": tn_n, "avg_launch_us": round(tn_ms * 1e3 / tn_n, 3) if tn_n else None,
+                            "share_of_step": round(tn_ms / 1e3 / t_dev, 4) if tn_n else None},
+        "roofline_fp64_gemm": {"kernel": "k_gemm_f64 (register-tiled DFMA GEMM)", "bound": "fp64",
+                               "achieved": round(ach_gf, 4) if ach_gf else None, "peak": FP64_NOMINAL_TFLOPS,
+                               "unit": "TFLOP/s", "frac": round(ach_gf / FP64_NOMINAL_TFLOPS, 4) if ach_gf else None,
+                               "peak_kind": "nominal (no FP64 figure in MEASURED_PEAKS.json)",
+                               "launches_per_step": gf_n,
+                               "avg_launch_us": round(gf_ms * 1e3 / gf_n, 3) if gf_n else None,
+                               "share_of_step": round(gf_ms / 1e3 / t_dev, 4) if gf_n else None},
         "clocks": clk.summary(),
     }
     if plain:
         line["plain_fp64"] = plain
+        line["speedup_vs_plain_fp64"] = round(plain["value"] / t_dev, 2)
     if grad_check:
         line["gradient_check"] = grad_check
-        line["speedup_vs_plain_fp64"] = round(plain["value"] / t_dev, 2)
     if not args.no_cpu_baseline:
-        cb, need = oracle_sample(w)
+        torch.set_num_threads(os.cpu_count() or 1)
+        cb, E_o, g_o, steps_o = oracle_full(w)
         line["cpu_baseline"] = {"value": round(cb, 3), "unit": "s", "cores": torch.get_num_threads(), "kind": "port",
-                                "sample": f"oracle (torch-CPU FP64): 4 CTMRG steps forward + reverse, scaled to the "
-                                          f"{need} steps it needs for |dE|<=1e-8"}
+                                "sample": f"one full oracle solve (torch-CPU FP64): {steps_o} CTMRG steps to the "
+                                          f"reference stop rule at tol {plain_tol(w):.3g}, energy, unrolled reverse; "
+                                          f"|dE| {abs(E_o - w['E_star']):.2e}"}
+        gv = {"oracle": "unrolled reverse of the oracle (the reference's Zygote gradient restated), same input",
+              "mixed_rel_l2": float(np.linalg.norm(g_h - g_o) / np.linalg.norm(g_o)),
+              "mixed_max_abs_rel": float(np.max(np.abs(g_h - g_o)) / np.max(np.abs(g_o)))}
+        if g_plain is not None:
+            gv["plain_rel_l2"] = float(np.linalg.norm(g_plain - g_o) / np.linalg.norm(g_o))
+            gv["plain_max_abs_rel"] = float(np.max(np.abs(g_plain - g_o)) / np.max(np.abs(g_o)))
+        line["gradient_vs_oracle"] = gv
     print(json.dumps(line), flush=True)
 
 
 # ---------------------------------------------------------------------------
-def oracle_sample(w, nsteps=4):
-    """Time the oracle on a bounded sample: nsteps CTMRG steps forward + reverse, scaled
-    to the oracle's own step count to reach the target (from its trajectory)."""
+def oracle_full(w):
+    """One full solve of workload w by the oracle on the host cores: energy
+    (CTMRG from :raw with the reference stop rule at the tolerance where its
+    trajectory is within TARGET of E*) and its unrolled reverse.  Returns
+    (seconds, E, dE/dA, CTMRG steps)."""
     import torch
     from oracle import tnad_oracle as orc
 
-    A = torch.as_tensor(workload_input(w)).requires_grad_(True)
-    h = torch.as_tensor(orc.hamiltonian_heisenberg())
+    h = orc.hamiltonian_heisenberg()
+    A = workload_input(w)
     t0 = time.perf_counter()
-    As = orc.indexperm_symmetrize(A)
-    ap, a = orc.double_layer(As)
-    C, T = orc.init_raw(a, w["chi"])
-    for _ in range(nsteps):
-        C, T, _ = orc.ctmrgstep(a, C, T)
-    e = orc.expectationvalue(h, ap, C, T)
-    torch.autograd.grad(e, A)
+    E, g, steps = orc.energy_and_grad(h, A, w["chi"], plain_tol(w), 400)
     dt = time.perf_counter() - t0
-    need = next(k + 1 for k, e_ in enumerate(w["energies"]) if abs(e_ - w["E_star"]) <= TARGET / 4)
-    return dt * need / nsteps, need
+    return dt, E, np.asarray(g).reshape(np.shape(A)), steps
 
 
 def run_reference(args):
+    """The reference's CPU path (the oracle restatement: Julia is absent) timed on
+    the host cores, every step one full energy + gradient solve of the workload.
+    The CPU needs no warm-up beyond the first call, so at most one warm-up solve
+    runs, which keeps the whole run within a few minutes."""
     import torch
 
     rank = int(os.environ.get("RANK", "0"))
@@ -388,22 +432,26 @@ def run_reference(args):
         return
     torch.set_num_threads(os.cpu_count() or 1)
     w = ESTAR[args.workload]
-    for _ in range(max(1, min(args.warmup, 1))):
-        oracle_sample(w, 2)
-    ts = []
+    nwarm = min(args.warmup, 1)
+    for _ in range(nwarm):
+        oracle_full(w)
+    ts, errs, steps = [], [], 0
     for _ in range(args.steps):
-        t, need = oracle_sample(w)
+        t, E, _, steps = oracle_full(w)
         ts.append(t)
+        errs.append(abs(E - w["E_star"]))
     v = statistics.mean(ts)
     cores = torch.get_num_threads()
+    sample = (f"full oracle solve per step (torch-CPU FP64, {cores} threads): {steps} CTMRG steps to the reference "
+              f"stop rule at tol {plain_tol(w):.3g}, energy and unrolled reverse; {nwarm} warm-up solve(s)")
     line = {
-        "metric": "CTMRG energy+gradient time to |dE|<=1e-8 vs FP64 oracle (D=4, chi=64)", "impl": "reference",
-        "value": round(v, 4), "unit": "s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+        "metric": metric_for(w), "impl": "reference",
+        "value": round(v, 4), "unit": "s", "n_gpus": 0, "steps": args.steps, "warmup": nwarm,
         "ms_per_step": round(v * 1e3, 1), "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic", "config": {"workload": args.workload, "D": w["D"], "chi": w["chi"]},
-        "cpu_baseline": {"value": round(v, 4), "unit": "s", "cores": cores, "kind": "port",
-                         "sample": f"4 CTMRG steps fwd+reverse (torch-CPU FP64) scaled to the {need} steps the "
-                                   f"oracle needs for |dE|<=1e-8"},
+        "dtype": "f64", "data": f"synthetic: {w['recipe']} site tensor (NumPy seed {w['seed']}), symmetrised",
+        "config": {"workload": args.workload, "D": w["D"], "chi": w["chi"], "phys": 2},
+        "delta_E": max(errs), "min": round(min(ts), 4), "max": round(max(ts), 4),
+        "cpu_baseline": {"value": round(v, 4), "unit": "s", "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": round(v, 4), "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

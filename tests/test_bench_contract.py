@@ -9,7 +9,13 @@ ROOT = Path(__file__).resolve().parent.parent
 
 
 def test_reference_arm_prints_one_contract_line():
-    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "1", "--warmup", "1"],
+    """Full oracle solves of the small D=2, chi=20 workload (the headline D=4
+    workload runs the same code, only longer)."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "2", "--warmup", "1",
+                        "--workload", "heisenberg_D2_chi20"],
                        capture_output=True, text=True, timeout=600, cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [l for l in r.stdout.splitlines() if l.strip().startswith("{")]
@@ -21,7 +27,11 @@ def test_reference_arm_prints_one_contract_line():
     assert d["impl"] == "reference" and d["higher_is_better"] is False and d["value"] > 0
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1 and d["cpu_baseline"]["sample"]
     assert d["e2e"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
-    assert d["config"]["workload"] == "heisenberg_D4_chi64"
+    assert d["config"]["workload"] == "heisenberg_D2_chi20"
+    # the GPU arm prints the same metric string for the same workload
+    assert d["metric"] == bench.metric_for(bench.ESTAR["heisenberg_D2_chi20"])
+    # every timed step is a full solve that reaches the target
+    assert d["delta_E"] <= bench.TARGET and d["steps"] == 2 and d["warmup"] == 1
 
 
 def test_gradient_check_compares_both_gradients_with_a_central_difference():

@@ -17,7 +17,7 @@
  *   model_tensor(::Ising,β)         src/exampletensors.jl:30-35
  *   trg(a,χ,niter;tol)              src/trg.jl:13-30   (+ Zygote adjoint)
  *   trg_svd                         src/trg.jl:33-44
- *   svd adjoint / svd_back          src/trg.jl:55-61, 72-106 (file lines 77-128)
+ *   svd adjoint / svd_back          src/trg.jl:55-61, 72-105
  *   ctmrg(rt;tol,maxit)             src/ctmrg.jl:110-117 + src/fixedpoint.jl:11-41
  *   ctmrgstep                       src/ctmrg.jl:126-153
  *   indexperm_symmetrize            src/ipeps.jl:32-39
@@ -137,7 +137,7 @@ int tnad_model_tensor_ising(double beta, double* a, double* da);
 int tnad_trg(tnad_ctx* ctx, const double* a, int d, int chi, int niter, double tol,
              double* lnZ, tnad_tape** tape);
 /* Pullback of trg: da = dlnZ · ∂lnZ/∂a  (Zygote adjoint of src/trg.jl:13-30 with
-   the SVD adjoint of src/trg.jl:55-128). */
+   the SVD adjoint of src/trg.jl:55-61, 72-105). */
 int tnad_trg_backward(tnad_ctx* ctx, tnad_tape* tape, double dlnZ, double* da);
 
 /* trg_svd(t, χ, tol) of src/trg.jl:33-44 for t of size d1×d2×d3×d4.
@@ -162,7 +162,7 @@ int tnad_svd(tnad_ctx* ctx, const double* A, int m, int n, double* U, double* S,
    device resolves that array's address and should come before any stream
    capture.  Sizes beyond 256 return TNAD_ERR_SHAPE. */
 int tnad_svd_noalloc(const double* A, int m, int n, double* U, double* S, double* V, void* stream);
-/* svd_back(U,S,V,dU,dS,dV; η) of src/trg.jl:94-128 (real).  dU/dS/dV may be NULL. */
+/* svd_back(U,S,V,dU,dS,dV; η) of src/trg.jl:72-105 (real).  dU/dS/dV may be NULL. */
 int tnad_svd_back(tnad_ctx* ctx, const double* U, const double* S, const double* V,
                   int m, int n, const double* dU, const double* dS, const double* dV,
                   double eta, double* dA);

@@ -12,7 +12,7 @@ Julia.  Gradients come from torch autograd, which reproduces Zygote's generic
 adjoints (einsum, permutedims, reshape, maximum, log); the two custom adjoints
 of the reference are restated exactly:
 
-* the SVD adjoint ``svd_back`` (src/trg.jl:77-128, Lorentzian eta = 1e-40);
+* the SVD adjoint ``svd_back`` (src/trg.jl:72-105, Lorentzian eta = 1e-40);
 * the norm adjoint  ``Δ·A/(‖A‖+eps(0f0))``      (src/autodiff.jl:23-29).
 
 Multi-tensor einsums of the reference are evaluated as pairwise contractions in
@@ -80,27 +80,27 @@ def norm(a):
 
 
 def svd_back(U, S, V, dU, dS, dV, eta: float = 1e-40):
-    """Real restatement of svd_back (src/trg.jl:94-128)."""
+    """Real restatement of svd_back (src/trg.jl:72-105)."""
     if dU is None and dS is None and dV is None:
         return None
     S2 = S * S
     Sinv = S / (S2 + eta)
-    F = S2[None, :] - S2[:, None]           # F[i,j] = s_j^2 - s_i^2   (:100)
-    F = F / (F * F + eta)                    # (:101)
+    F = S2[None, :] - S2[:, None]           # F[i,j] = s_j^2 - s_i^2   (:78)
+    F = F / (F * F + eta)                    # (:79)
     res = torch.zeros(S.shape[0], S.shape[0], dtype=S.dtype)
     if dU is not None:
-        J = F * (U.T @ dU)                   # (:105-106)
-        res = res + (J + J.T) * S[None, :]   # (J+J')*Diagonal(S); imag term is 0 for real
+        J = F * (U.T @ dU)                   # (:83-84)
+        res = res + (J + J.T) * S[None, :]   # (:85) (J+J')*Diagonal(S); imag term is 0 for real
     if dV is not None:
-        K = F * (V.T @ dV)                   # (:110-111)
+        K = F * (V.T @ dV)                   # (:88-89)
         res = res + S[:, None] * (K + K.T)
     if dS is not None:
-        res = res + torch.diag(dS)           # (:115)
-    out = U @ res @ V.T                      # (:118)
+        res = res + torch.diag(dS)           # (:93)
+    out = U @ res @ V.T                      # (:96)
     if dU is not None and U.shape[0] != U.shape[1]:
-        out = out + ((dU - U @ (U.T @ dU)) * Sinv[None, :]) @ V.T          # (:120-122)
+        out = out + ((dU - U @ (U.T @ dU)) * Sinv[None, :]) @ V.T          # (:98-99)
     if dV is not None and V.shape[0] != V.shape[1]:
-        out = out + (U * Sinv[None, :]) @ (dV.T - (dV.T @ V) @ V.T)          # (:124-126)
+        out = out + (U * Sinv[None, :]) @ (dV.T - (dV.T @ V) @ V.T)          # (:102-103)
     return out
 
 

@@ -128,7 +128,7 @@ def _trg(a, chi, niter, tol, record):
 
 
 def trg_gradient(a, chi: int, niter: int, tol: float = 1e-16, dlnZ: float = 1.0):
-    """(lnZ, ∂lnZ/∂a): the Zygote gradient of trg (src/trg.jl:13-30, 55-128)."""
+    """(lnZ, ∂lnZ/∂a): the Zygote gradient of trg (src/trg.jl:13-30, 55-61, 72-105)."""
     a = farr(a)
     lnZ, tp = _trg(a, chi, niter, tol, record=True)
     g = fzeros(a.shape)
@@ -171,7 +171,7 @@ def svd(A):
 
 
 def svd_back(U, S, V, dU=None, dS=None, dV=None, eta: float = 1e-40):
-    """SVD adjoint (src/trg.jl:94-128) on the GPU."""
+    """SVD adjoint (src/trg.jl:72-105) on the GPU."""
     U, S, V = farr(U), farr(S), farr(V)
     m, n = U.shape
     dA = fzeros((m, n))
@@ -430,9 +430,10 @@ def optimiseipeps(ipeps: IPEPS, h, chi: int, tol: float, maxit: int, f_tol: floa
 def num_grad(f, K, delta: float = 1e-5, dist=None):
     """(f(K+δ/2) − f(K−δ/2))/δ, elementwise for arrays (src/autodiff.jl:44-63).
 
-    dist: an initialised torch.distributed process group (one rank per GPU).
-    The elements are then independent units: each rank differentiates a
-    contiguous share of them and every rank returns the gathered array."""
+    dist: the ``torch.distributed`` module itself, with its default process
+    group initialised (one rank per GPU).  The elements are then independent
+    units: each rank differentiates a contiguous share of them and every rank
+    returns the gathered array."""
     if np.isscalar(K):
         return (f(K + delta / 2) - f(K - delta / 2)) / delta
     K = np.asarray(K, dtype=np.float64)

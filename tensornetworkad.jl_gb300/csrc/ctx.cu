@@ -1,4 +1,5 @@
 // Context, device workspace and error plumbing of libtnad.
+#include <cstdlib>
 #include <cstring>
 
 #include "tnad_internal.h"
@@ -117,6 +118,10 @@ extern "C" int tnad_ctx_create(tnad_ctx** out, int device) {
     TNAD_CK(cudaMalloc(&c->d_flag, 64 * sizeof(int)));
     TNAD_CK(cudaMallocHost(&c->h_flag, 64 * sizeof(int)));
     TNAD_CK(cudaMemsetAsync(c->d_flag, 0, 64 * sizeof(int), c->stream));
+    if (const char* f = std::getenv("TNAD_TEST_FAULT")) {
+      if (!std::strcmp(f, "tc_withhold")) c->fault_once = kFaultTcWithhold;
+      if (!std::strcmp(f, "jacobi_cap")) c->fault_once = kFaultJacobiCap;
+    }
   } catch (const Error& e) {
     int code = e.code;
     tnad_ctx_destroy(c);

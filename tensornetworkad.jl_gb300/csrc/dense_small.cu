@@ -303,7 +303,7 @@ void eigh_small(tnad_ctx* c, const double* A, int64_t p, double* W, double* lam)
 
 // ---------------------------------------------------------------- polar factor
 // O = polar(X) for a χ×χ X (χ ≤ 128) by Newton–Schulz, O ← O·(3I − OᵀO)/2,
-// in FP32 in one CTA (the caller polishes in FP64).  info[0] = 1 when the
+// in FP32 in one CTA (the caller polishes in FP64); larger χ take polar_ns_gemm.  info[0] = 1 when the
 // result is orthogonal to 1e-4 (else the caller falls back to sign alignment).
 __global__ void k_polar_ns(const double* __restrict__ X, int m, int iters, double* __restrict__ O,
                            int* __restrict__ info) {
@@ -398,8 +398,52 @@ __global__ void k_polar_ns(const double* __restrict__ X, int m, int iters, doubl
   if (threadIdx.x == 0) info[0] = worst < 1e-4f ? 1 : 0;
 }
 
+// info[0] = 1 when max |G − I| < 1e-4 for the m×m matrix G = OᵀO (one CTA)
+__global__ void k_orth_info(const double* __restrict__ G, int64_t m, int* __restrict__ info) {
+  __shared__ double red[32];
+  double dev = 0.0;
+  for (int64_t e = threadIdx.x; e < m * m; e += blockDim.x)
+    dev = fmax(dev, fabs(G[e] - ((e % m) == (e / m) ? 1.0 : 0.0)));
+  for (int o = 16; o > 0; o >>= 1) dev = fmax(dev, __shfl_xor_sync(0xffffffffu, dev, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = dev;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t = fmax(t, red[w]);
+    info[0] = t < 1e-4 ? 1 : 0;
+  }
+}
+
+// Polar factor for m > 128 (beyond one CTA's shared memory): the same
+// Newton–Schulz iteration O ← O·(3I − OᵀO)/2 from O = 0.999·X (X is a product of
+// two orthonormal bases, so its singular values are ≤ 1), with its products on
+// the multi-CTA GEMMs (TF32X3 where the tensor cores are available; the caller
+// polishes in FP64), and the same orthogonality flag.
+static void polar_ns_gemm(tnad_ctx* c, const double* X, int64_t m, int iters, double* O, int* dev_info) {
+  WsScope scope(c);
+  double* G = ws_d(c, m * m);
+  double* O2 = ws_d(c, m * m);
+  const int pr = c->tc_ok ? TNAD_PREC_TF32X3 : TNAD_PREC_FP64;
+  copy_d2d(c, O, X, m * m);
+  scale(c, m * m, 0.999, O);
+  for (int it = 0; it < iters; ++it) {
+    gemm(c, pr, 'T', 'N', m, m, m, 1.0, O, m, O, m, 0.0, G, m);
+    copy_d2d(c, O2, O, m * m);
+    gemm(c, pr, 'N', 'N', m, m, m, -0.5, O, m, G, m, 1.5, O2, m);
+    copy_d2d(c, O, O2, m * m);
+  }
+  gemm(c, pr, 'T', 'N', m, m, m, 1.0, O, m, O, m, 0.0, G, m);
+  k_orth_info<<<1, 1024, 0, c->stream>>>(G, m, dev_info);
+  count_launch(c);
+  check_launch(c, "polar_ns_gemm");
+}
+
 void polar_ns(tnad_ctx* c, const double* X, int64_t m, int iters, double* O, int* dev_info) {
-  TNAD_REQUIRE(m >= 1 && m <= 128, TNAD_ERR_SHAPE, "polar_ns: m must be in [1,128]");
+  TNAD_REQUIRE(m >= 1, TNAD_ERR_SHAPE, "polar_ns: m must be >= 1");
+  if (m > 128) {
+    polar_ns_gemm(c, X, m, iters, O, dev_info);
+    return;
+  }
   static std::atomic<bool> attr{false};
   if (!attr) {
     TNAD_CK(cudaFuncSetAttribute(k_polar_ns, cudaFuncAttributeMaxDynamicSharedMemorySize, 3 * 129 * 128 * 4));

@@ -66,12 +66,12 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
   return ok != 0;
 }
 
-// bounded wait: false (and *err set) after ~2 s
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code) {
+// bounded wait: false (and *err set) after limit_ns (2 s in normal operation)
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code, uint64_t limit_ns) {
   if (mbar_try(bar, parity)) return true;
   uint64_t t0 = gtime();
   while (!mbar_try(bar, parity)) {
-    if (gtime() - t0 > 2000000000ull) {
+    if (gtime() - t0 > limit_ns) {
       atomicExch(err, code);
       return false;
     }
@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(128, 1)
     k_gemm_tc(const __grid_constant__ CUtensorMap tAh, const __grid_constant__ CUtensorMap tAl,
               const __grid_constant__ CUtensorMap tBh, const __grid_constant__ CUtensorMap tBl, int M, int N,
               int kblocks_total, int kps, double alpha, double beta, OutT* __restrict__ C, int64_t ldc,
-              double* __restrict__ P, int* err) {
+              double* __restrict__ P, int* err, uint64_t wait_ns, int withhold_first) {
   using CF = Cfg<BN, SPLIT>;
   // split-K: CTA z owns K slices [kbeg, kbeg + kblocks); with P != null it
   // writes its raw FP32 sum as an FP64 partial, reduced in FP64 afterwards
@@ -178,12 +178,15 @@ __global__ void __launch_bounds__(128, 1)
     for (int kb = 0; kb < kblocks; ++kb) {
       const int s = kb % STAGES;
       const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
-      if (kb >= STAGES && !mbar_wait(empty0 + 8 * s, ph ^ 1u, err, 1)) break;
+      if (kb >= STAGES && !mbar_wait(empty0 + 8 * s, ph ^ 1u, err, 1, wait_ns)) break;
       uint8_t* st = smem + s * CF::STAGE;
       const uint32_t fb = full0 + 8 * s;
       mbar_expect_tx(fb, (uint32_t)CF::STAGE);
       const int kx = (kbeg + kb) * CF::KSLICE;
-      if (SPLIT) {
+      if (withhold_first && kb == 0) {
+        // failure-path test: the slice's bytes are expected but never loaded,
+        // so every wait on this stage runs out; no copy is in flight for it
+      } else if (SPLIT) {
         tma_load_2d(su32(st), &tAh, kx, m0, fb);
         tma_load_2d(su32(st + TILE_A), &tAl, kx, m0, fb);
         tma_load_2d(su32(st + 2 * TILE_A), &tBh, kx, n0, fb);
@@ -196,7 +199,7 @@ __global__ void __launch_bounds__(128, 1)
     }
     // make sure none of this CTA's copies is still in flight when it exits
     for (int kb = (issued > STAGES ? issued - STAGES : 0); kb < issued; ++kb)
-      mbar_wait(full0 + 8 * (kb % STAGES), (uint32_t)(kb / STAGES) & 1u, err, 2);
+      mbar_wait(full0 + 8 * (kb % STAGES), (uint32_t)(kb / STAGES) & 1u, err, 2, wait_ns);
   } else if (warp == 1 && lane == 0) {
     // ---------------- MMA issuer ----------------
     // instruction descriptor: D = F32; A, B = TF32 (kind::tf32) or BF16 (kind::f16); both K-major
@@ -207,7 +210,7 @@ __global__ void __launch_bounds__(128, 1)
     for (int kb = 0; kb < kblocks && ok; ++kb) {
       const int s = kb % STAGES;
       const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
-      if (!mbar_wait(full0 + 8 * s, ph, err, 3)) {
+      if (!mbar_wait(full0 + 8 * s, ph, err, 3, wait_ns)) {
         ok = false;
         break;
       }
@@ -238,7 +241,7 @@ __global__ void __launch_bounds__(128, 1)
   __syncwarp();
 
   // ---------------- epilogue: TMEM → registers → FP64 global ----------------
-  const bool okd = mbar_wait(done, 0u, err, 4);
+  const bool okd = mbar_wait(done, 0u, err, 4, wait_ns);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const int row = m0 + warp * 32 + lane;
   const bool err_set = (*(volatile int*)err) != 0;
@@ -407,9 +410,16 @@ void launch_tc(tnad_ctx* c, int64_t M, int64_t N, int64_t K, double alpha, void*
   int* err = c->d_flag + 8;
   WsScope scope(c);
   double* P = splits > 1 ? ws_d(c, (int64_t)splits * M * N) : nullptr;
+  int withhold = 0;
+  uint64_t wait_ns = 2000000000ull;
+  if (c->fault_once == kFaultTcWithhold) {
+    withhold = 1;
+    wait_ns = 20000000ull;
+    c->fault_once = kFaultNone;
+  }
   KernelTimer kt(c, timer_name, 2.0 * (double)M * (double)N * (double)K);  // logical flops
   k_gemm_tc<BN, SPLIT, OutT><<<grid, 128, CF::SMEM, c->stream>>>(tAh, tAl, tBh, tBl, (int)M, (int)N, kbt, kps, alpha,
-                                                                 beta, Cm, ldc, P, err);
+                                                                 beta, Cm, ldc, P, err, wait_ns, withhold);
   count_launch(c);
   check_launch(c, timer_name);
   if (P) {

@@ -509,7 +509,12 @@ void svd_jacobi(tnad_ctx* c, const double* A, int64_t m, int64_t n, double* U, d
   }
   SweepGraph<double> sweep64;
   int prev_rot = 0;
-  for (int sweep = 0; sweep < kMaxSweeps && !converged; ++sweep) {
+  int max_sweeps = kMaxSweeps;
+  if (c->fault_once == kFaultJacobiCap) {  // failure-path test: one sweep only
+    max_sweeps = 1;
+    c->fault_once = kFaultNone;
+  }
+  for (int sweep = 0; sweep < max_sweeps && !converged; ++sweep) {
     // Purely relative sweeps first (rel_sweeps of them): they drive null and
     // noise-level columns to exact orthogonality (the triplets trg_svd's √s
     // pullback relies on).  Afterwards, or from the start for rel_sweeps = 0,
@@ -635,17 +640,22 @@ static double* noalloc_scratch_addr(int dev) {
 // Thin SVD A = U·diag(S)·Vᵀ (m ≥ n, n ≤ m ≤ 256) by the same one-sided Jacobi
 // kernels as tnad_svd, without any device allocation: for callers that cannot
 // call cudaMalloc (a host framework that owns all device memory through its own
-// allocator, code running while a CUDA graph is being built by someone else,
-// or a latency-critical loop where an allocation would synchronise the device).
-// A, U, S, V are DEVICE pointers (m×n, n, n×n, column-major); stream may be 0.
-// The first call on a device resolves the scratch address for that device and
-// should therefore happen before any stream capture.  Returns TNAD_ERR_SHAPE
-// for m or n beyond 256 (the static scratch's limit), TNAD_ERR_ARG for null
-// pointers or m < n, TNAD_ERR_NOT_CONVERGED / TNAD_ERR_CUDA as tnad_svd does.
+// allocator, or a latency-critical loop where an allocation would synchronise
+// the device).  A, U, S, V are DEVICE pointers (m×n, n, n×n, column-major);
+// stream may be 0.  The call waits for its stream once per Jacobi sweep (it
+// reads the sweep's rotation count on the host).  The first call on a device
+// resolves the scratch address for that device and should therefore happen
+// before any stream capture; the cached address is not re-resolved after a
+// cudaDeviceReset.  A launch error that earlier, unrelated work left pending
+// is cleared on entry, so that only this call's own launches are reported.
+// Returns TNAD_ERR_SHAPE for m or n beyond 256 (the static scratch's limit),
+// TNAD_ERR_ARG for null pointers or m < n, TNAD_ERR_NOT_CONVERGED /
+// TNAD_ERR_CUDA as tnad_svd does.
 extern "C" int tnad_svd_noalloc(const double* A, int m, int n, double* U, double* S, double* V, void* stream) {
   using namespace tnad;
   if (!A || !U || !S || !V || n < 1 || m < n) return TNAD_ERR_ARG;
   if (m > kNoAllocMax || n > kNoAllocMax) return TNAD_ERR_SHAPE;
+  (void)cudaGetLastError();
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return TNAD_ERR_CUDA;
   double* base = noalloc_scratch_addr(dev);

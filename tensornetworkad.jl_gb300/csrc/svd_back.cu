@@ -1,4 +1,4 @@
-// SVD adjoint of src/trg.jl:94-128 (real case).  The Lorentzian-broadened
+// SVD adjoint of src/trg.jl:72-105 (real case).  The Lorentzian-broadened
 // F-matrix F_ij = (s_j²−s_i²)/((s_j²−s_i²)²+η) is formed in FP64 inside the
 // kernel that assembles res = (J+Jᵀ)S + S(K+Kᵀ) + diag(dS); the surrounding
 // products Uᵀ·dU, Vᵀ·dV, U·res·Vᵀ are GEMMs.
@@ -120,7 +120,7 @@ void svd_back(tnad_ctx* c, int prec, const double* U, const double* S, const dou
   gemm(c, prec, 'N', 'N', m, n, n, 1.0, U, m, res, n, 0.0, T1, m);
   gemm(c, prec, 'N', 'T', m, n, n, 1.0, T1, m, V, n, 0.0, dA, m);
   if (dU && m != n) {
-    // (dU − U·(Uᵀ·dU))·diag(Sinv)·Vᵀ   src/trg.jl:120-122
+    // (dU − U·(Uᵀ·dU))·diag(Sinv)·Vᵀ   src/trg.jl:98-99
     double* P = ws_d(c, m * n);
     copy_d2d(c, P, dU, m * n);
     gemm(c, prec, 'N', 'N', m, n, n, -1.0, U, m, X, n, 1.0, P, m);

@@ -82,6 +82,15 @@ struct tnad_ctx {
   int* d_flag = nullptr;    // device flags / counters (64 ints)
   int* h_flag = nullptr;    // pinned host mirror of the flags
   bool tc_ok = false;       // tcgen05 GEMM path available (sm_100 family)
+  // One-shot fault injection for the failure-path tests, set from the
+  // environment variable TNAD_TEST_FAULT when the context is created:
+  //   kFaultTcWithhold — the next tensor-core GEMM launch does not issue the TMA
+  //     loads of its first K slice and waits at most 20 ms on an mbarrier, so
+  //     the bounded wait runs out (TNAD_ERR_TIMEOUT) with no copy in flight;
+  //   kFaultJacobiCap — the next Jacobi SVD is capped at one FP64 sweep
+  //     (TNAD_ERR_NOT_CONVERGED).
+  // Each is cleared when used; later calls on the context run normally.
+  int fault_once = 0;
   // kernel timer (tnad_ctx_kernel_timer): events around every launch of one
   // kernel family, with the algorithmic work (flops or bytes) of each launch
   std::string ktimer;
@@ -96,6 +105,8 @@ struct tnad_ctx {
 };
 
 namespace tnad {
+
+enum { kFaultNone = 0, kFaultTcWithhold = 1, kFaultJacobiCap = 2 };
 
 // Phase timer: with TNAD_TRACE set in the environment, CUDA events bracket
 // named phases on the context stream and a per-phase summary goes to stderr

@@ -1,5 +1,5 @@
 // TRG on the device: trg (src/trg.jl:13-30), trg_svd (src/trg.jl:33-44) and the
-// reverse pass (Zygote adjoint of the same loop with svd_back, src/trg.jl:55-128).
+// reverse pass (Zygote adjoint of the same loop with svd_back, src/trg.jl:55-61, 72-105).
 // The bond dimension follows the reference exactly, including its
 // searchsortedfirst quirk: k = min(#(s > tol) + 1, χ, length(s)).
 #include <cmath>

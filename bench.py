@@ -57,6 +57,9 @@ def parse():
     p.add_argument("--n-held", dest="n_held", type=int, default=500, help="held-out tensors")
     p.add_argument("--train-steps", dest="train_steps", type=int, default=6000)
     p.add_argument("--threads", type=int, default=8, help="concurrent CTMRG runs while generating targets")
+    p.add_argument("--lbfgs-steps", dest="lbfgs_steps", type=int, default=20, help="optimise_* workloads")
+    p.add_argument("--chi", type=int, default=0, help="optimise_* workloads: bond dimension (default 64)")
+    p.add_argument("--only", default=None, help="optimise_* workloads: run one mode only")
     p.add_argument("--profile", default=None, choices=["solve", "mlp"],
                    help="run one untimed solve of the workload (solve) or 20 training steps of the D=3, chi=36 "
                         "warm-start network (mlp) and exit: the command profiled by ncu")
@@ -607,6 +610,76 @@ def run_learned_headline(args):
     print(json.dumps(line), flush=True)
 
 
+def run_optimise(args):
+    """optimiseipeps (src/variationalipeps.jl:67-75) at D=4 on the GPU: L-BFGS
+    (m = 20) from the headline workload's site tensor for --lbfgs-steps
+    iterations, once with the mixed path (implicit fixed-point adjoint) and once
+    with the unrolled reverse checkpointed at every step (tape_budget 0: only
+    (C, T) of each step is kept; each step's decomposition is recomputed in the
+    reverse pass), TF32X3 contractions and the FP64 Jacobi SVD.  Reports the
+    energy after every iteration, wall time, evaluations and the device memory
+    in use at the end of every forward pass (cudaMemGetInfo)."""
+    import ctypes as C
+
+    import scipy.optimize
+    import torch
+    import __graft_entry__ as ge
+
+    tn = ge.load_package()
+    torch.cuda.set_device(0)
+    chi = args.chi or 64
+    w = ESTAR["heisenberg_D4_chi64"]
+    A0 = workload_input(w)
+    h = tn.hamiltonian(tn.Heisenberg())
+    shape = A0.shape
+    free0, total = torch.cuda.mem_get_info()
+    modes = {
+        "mixed": (tn.mixed_opts(), 3e-8),
+        "checkpointed_unrolled": (tn.default_opts(prec=tn._lib.PREC_TF32X3, solver=tn._lib.SOLVER_FULL_SVD,
+                                                  adjoint=tn._lib.ADJOINT_UNROLLED, tape_budget=0),
+                                  plain_tol(w) if chi == 64 else 1e-7),
+    }
+    out = {}
+    for name, (opts, tol) in modes.items():
+        if args.only and name != args.only:
+            continue
+        evals, energies, peak, last = [0], [], [0], [None]
+
+        def fg(x):
+            r = tn._energy(h, tn.SquareIPEPS(x.reshape(shape, order="F")), chi, tol, 400, opts, record=True)
+            last[0] = r.E
+            free, _ = torch.cuda.mem_get_info()
+            peak[0] = max(peak[0], total - free)
+            g = tn.fzeros(shape)
+            cc = r.tape.c
+            cc.check(cc.lib.tnad_energy_backward(cc.h, r.tape.h, 1.0, tn.ptr(g)))
+            evals[0] += 1
+            return r.E, np.asarray(g).ravel(order="F")
+
+        fg(np.asarray(A0).ravel(order="F"))  # warm-up evaluation (first-call costs), not counted
+        evals[0] = 0
+        t0 = time.perf_counter()
+        res = scipy.optimize.minimize(fg, np.asarray(A0).ravel(order="F"), jac=True, method="L-BFGS-B",
+                                      callback=lambda xk: energies.append(last[0]),
+                                      options=dict(maxcor=20, maxiter=args.lbfgs_steps, ftol=0.0, gtol=0.0))
+        dt = time.perf_counter() - t0
+        # the energy after every iteration, re-evaluated from the iterates' record
+        out[name] = {"iterations": int(res.nit), "evaluations": evals[0], "seconds": round(dt, 2),
+                     "s_per_evaluation": round(dt / max(evals[0], 1), 3), "E_final": float(res.fun),
+                     "E_per_iteration": energies,
+                     "E_start": None, "peak_device_bytes": int(peak[0] - (total - free0)),
+                     "workspace_bytes": int(tn.ctx().lib.tnad_ctx_workspace_bytes(tn.ctx().h)),
+                     "stop_tol": tol, "message": str(res.message)}
+    E_start = tn.energy(h, tn.SquareIPEPS(A0), chi, 1e-10, 400, tn.mixed_opts())
+    for v in out.values():
+        v["E_start"] = E_start
+    line = {"metric": f"optimiseipeps: {args.lbfgs_steps} L-BFGS iterations at D=4, chi={chi} (Heisenberg)",
+            "unit": "s", "higher_is_better": False, "config": {"workload": f"optimise_D4_chi{chi}", "D": 4,
+                                                              "chi": chi, "lbfgs_m": 20},
+            "data": "synthetic: the headline N(0,1) site tensor as the start", "modes": out}
+    print(json.dumps(line), flush=True)
+
+
 def run_profile(args):
     import importlib
 
@@ -635,6 +708,8 @@ if __name__ == "__main__":
         run_profile(a)
     elif a.impl == "reference":
         run_reference(a)
+    elif a.workload.startswith("optimise"):
+        run_optimise(a)
     elif a.workload == "learned_D4_chi64":
         run_learned_headline(a)
     elif a.workload.startswith("learned"):

@@ -53,7 +53,10 @@ enum {
 enum {
   TNAD_PREC_FP64 = 0,   /* DFMA tiles: the plain FP64 path                           */
   TNAD_PREC_TF32X3 = 1, /* tcgen05 kind::tf32, 3 split products, FP32 accumulation    */
-  TNAD_PREC_LADDER = 2  /* TF32X3 until the residual stalls, then FP64 polishing      */
+  TNAD_PREC_LADDER = 2, /* TF32X3 until the residual stalls, then FP64 polishing      */
+  TNAD_PREC_FP64_TC = 3 /* tnad_gemm only: FP64-accurate products from six BF16 slices
+                           per operand on the tcgen05 tensor cores (about 2^-47 of
+                           the row/column scales; no reference counterpart)           */
 };
 
 /* Eigen/SVD solver used for the CTMRG projector. */
@@ -86,7 +89,10 @@ typedef struct tnad_opts {
   int32_t stop_rule;       /* 0: reference StopFunction on all χd values;
                               1: ‖Δ(top-χ values)‖₂ ≤ tol (subspace solver)       */
   int32_t fp_maxit;        /* fixed-point adjoint iteration cap                   */
-  int32_t reserved0;
+  int32_t fp64_tc;         /* 1: the FP64 products of this call (the FP64 phase of
+                              the ladder, the fixed-point adjoint's FP64 operator)
+                              run as tensor-core FP64 emulation (TNAD_PREC_FP64_TC)
+                              instead of DFMA tiles; 0 (default): DFMA             */
   double fp_tol;           /* fixed-point adjoint relative residual target        */
   double ladder_tol;       /* LADDER: residual where TF32X3 hands over to FP64   */
   int64_t tape_budget;     /* bytes of per-step tape kept on device; beyond it
@@ -116,7 +122,8 @@ void tnad_tape_free(tnad_tape* tape);
 
 /* -------- building blocks (the role OMEinsum plays in the reference) -------- */
 /* Column-major C(M×N) = alpha·op(A)·op(B) + beta·C with op ∈ {'N','T'}; prec is
-   TNAD_PREC_FP64 (DFMA) or TNAD_PREC_TF32X3 (tcgen05).  Host pointers. */
+   TNAD_PREC_FP64 (DFMA), TNAD_PREC_TF32X3 or TNAD_PREC_FP64_TC (tcgen05).  Host
+   pointers. */
 int tnad_gemm(tnad_ctx* ctx, int prec, char ta, char tb, int64_t M, int64_t N, int64_t K, double alpha,
               const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc);
 /* Pairwise contraction C[lc] = Σ A[la]·B[lb] (the pairwise form of ein"la,lb -> lc"

@@ -400,11 +400,13 @@ def tape_stats(tape) -> dict:
     return out
 
 
-def mixed_opts(ladder_tol: float = 1e-5, fp_tol: float = 1e-9, fp_maxit: int = 200, **kw) -> L.Opts:
-    """Options of the mixed path: TF32X3 contractions with the FP64 polishing ladder,
-    the warm-started subspace solver, and the implicit fixed-point adjoint."""
+def mixed_opts(ladder_tol: float = 1e-5, fp_tol: float = 1e-9, fp_maxit: int = 200, fp64_tc: int = 1,
+               **kw) -> L.Opts:
+    """Options of the mixed path: TF32X3 contractions with the FP64 polishing ladder
+    (whose FP64 products run as tensor-core FP64 emulation when fp64_tc = 1), the
+    warm-started subspace solver, and the implicit fixed-point adjoint."""
     return default_opts(prec=L.PREC_LADDER, solver=L.SOLVER_SUBSPACE, adjoint=L.ADJOINT_FIXEDPOINT, stop_rule=1,
-                        ladder_tol=ladder_tol, fp_tol=fp_tol, fp_maxit=fp_maxit, **kw)
+                        ladder_tol=ladder_tol, fp_tol=fp_tol, fp_maxit=fp_maxit, fp64_tc=fp64_tc, **kw)
 
 
 def optimiseipeps(ipeps: IPEPS, h, chi: int, tol: float, maxit: int, f_tol: float = 1e-6, iterations: int = 1000,

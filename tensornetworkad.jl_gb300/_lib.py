@@ -21,7 +21,7 @@ ERRORS = {
     -1: "TNAD_ERR_ARG", -2: "TNAD_ERR_SHAPE", -3: "TNAD_ERR_CUDA", -4: "TNAD_ERR_NOT_CONVERGED",
     -5: "TNAD_ERR_NONFINITE", -6: "TNAD_ERR_NOMEM", -7: "TNAD_ERR_STATE", -8: "TNAD_ERR_TIMEOUT",
 }
-PREC_FP64, PREC_TF32X3, PREC_LADDER = 0, 1, 2
+PREC_FP64, PREC_TF32X3, PREC_LADDER, PREC_FP64_TC = 0, 1, 2, 3
 WARM_NONE, WARM_GIVEN, WARM_LEARNED = 0, 1, 2
 SOLVER_FULL_SVD, SOLVER_SUBSPACE = 0, 1
 ADJOINT_UNROLLED, ADJOINT_FIXEDPOINT = 0, 1
@@ -40,7 +40,7 @@ class DimensionMismatch(ValueError):
 class Opts(C.Structure):
     _fields_ = [
         ("prec", C.c_int32), ("solver", C.c_int32), ("adjoint", C.c_int32), ("device_ptrs", C.c_int32),
-        ("warm_start", C.c_int32), ("stop_rule", C.c_int32), ("fp_maxit", C.c_int32), ("reserved0", C.c_int32),
+        ("warm_start", C.c_int32), ("stop_rule", C.c_int32), ("fp_maxit", C.c_int32), ("fp64_tc", C.c_int32),
         ("fp_tol", C.c_double), ("ladder_tol", C.c_double), ("tape_budget", C.c_int64),
     ]
 

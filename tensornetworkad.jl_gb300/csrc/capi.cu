@@ -105,7 +105,8 @@ extern "C" int tnad_gemm(tnad_ctx* c, int prec, char ta, char tb, int64_t M, int
   const double* dB = to_dev(c, B, nbb, false);
   double* dC = ws_d(c, ldc * N);
   TNAD_CK(cudaMemcpyAsync(dC, Cm, ldc * N * 8, cudaMemcpyHostToDevice, c->stream));
-  TNAD_REQUIRE(prec == TNAD_PREC_FP64 || prec == TNAD_PREC_TF32X3, TNAD_ERR_ARG, "tnad_gemm: prec");
+  TNAD_REQUIRE(prec == TNAD_PREC_FP64 || prec == TNAD_PREC_TF32X3 || prec == TNAD_PREC_FP64_TC, TNAD_ERR_ARG,
+               "tnad_gemm: prec");
   gemm(c, prec, ta, tb, M, N, K, alpha, dA, lda, dB, ldb, beta, dC, ldc);
   to_host(c, Cm, dC, ldc * N, false);
   finish_call(c);
@@ -309,6 +310,7 @@ extern "C" int tnad_ctmrg(tnad_ctx* c, const double* bulk, int d, int chi, const
   copy_d2d(c, wC, to_dev(c, C0, (int64_t)chi * chi, dev), (int64_t)chi * chi);
   copy_d2d(c, wT, to_dev(c, T0, (int64_t)chi * d * chi, dev), (int64_t)chi * d * chi);
   int prec = o.prec == TNAD_PREC_FP64 ? TNAD_PREC_FP64 : TNAD_PREC_TF32X3;
+  Fp64TcScope fp64_route(c, o.fp64_tc != 0);
   CtmrgRun run = ctmrg_run(c, prec, a, d, chi, wC, wT, tol, maxit, tape ? &own->tape : nullptr, &own->pool,
                            o.tape_budget);
   if (steps) *steps = run.steps;

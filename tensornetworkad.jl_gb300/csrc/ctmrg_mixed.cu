@@ -134,7 +134,7 @@ void align_polar(tnad_ctx* c, int prec, double* z, const double* zprev, int64_t 
   double* O = ws_d(c, (int64_t)chi * chi);
   double* zp = ws_d(c, n * chi);
   int* ok = c->d_flag + 18;
-  gemm_f64(c, 'T', 'N', chi, chi, n, 1.0, z, n, zprev, n, 0.0, X, chi);
+  gemm(c, TNAD_PREC_FP64, 'T', 'N', chi, chi, n, 1.0, z, n, zprev, n, 0.0, X, chi);
   polar_ns(c, X, chi, 24, O, ok);
   ns_polish_f64(c, O, chi, 2);
   gemm(c, prec, 'N', 'N', n, chi, chi, 1.0, z, n, O, chi, 0.0, zp, n);
@@ -162,7 +162,7 @@ void cholqr2(tnad_ctx* c, int prec, const double* Y, int64_t n, int64_t p, doubl
   }
   const double* src = t;
   for (int pass = 0; pass < 2; ++pass) {
-    gemm_f64(c, 'T', 'N', p, p, n, 1.0, src, n, src, n, 0.0, G, p);
+    gemm(c, TNAD_PREC_FP64, 'T', 'N', p, p, n, 1.0, src, n, src, n, 0.0, G, p);
     // the second Gram matrix is I + O(κ(Y)²·ε64): at TF32X3 accuracy its
     // factor is taken in FP32 (GB300's FP32 pipe is far wider than its FP64 one)
     if (pass == 1 && prec != TNAD_PREC_FP64)
@@ -270,7 +270,7 @@ MixedRun ctmrg_run_mixed(tnad_ctx* c, const double* a_, int d, int chi, double* 
     }
     // Rayleigh–Ritz in span(Q)
     tr.mark(prec == TNAD_PREC_FP64 ? "ritz_f64" : "ritz_tf32");
-    gemm_f64(c, 'T', 'N', p, p, n, 1.0, Q, n, Y, n, 0.0, H, p);
+    gemm(c, TNAD_PREC_FP64, 'T', 'N', p, p, n, 1.0, Q, n, Y, n, 0.0, H, p);
     k_symmetrize_small<<<nb(p * p), 256, 0, c->stream>>>(H, (int)p);
     count_launch(c);
     if (prec == TNAD_PREC_FP64)

@@ -225,6 +225,8 @@ void double_layer_bwd(tnad_ctx* c, int prec, const double* As, int D, int s, dou
 
 void energy_fwd(tnad_ctx* c, EnergyTape& tp, const double* h, const double* A, int D, int s, int chi, double tol,
                 int maxit, const tnad_opts& o, const double* Cinit, const double* Tinit, bool record) {
+  tp.fp64_tc = o.fp64_tc != 0;
+  Fp64TcScope fp64_route(c, tp.fp64_tc);
   const int d = D * D;
   const int64_t nA = (int64_t)D * D * D * D * s;
   const int64_t nap = (int64_t)d * d * d * d * s * s;
@@ -326,6 +328,7 @@ void energy_fwd(tnad_ctx* c, EnergyTape& tp, const double* h, const double* A, i
 }
 
 void energy_bwd(tnad_ctx* c, EnergyTape& tp, double dE, double* dA) {
+  Fp64TcScope fp64_route(c, tp.fp64_tc);
   const int D = tp.D, s = tp.s, chi = tp.chi, d = tp.d;
   const int64_t nap = (int64_t)d * d * d * d * s * s;
   const int64_t d4 = (int64_t)d * d * d * d;

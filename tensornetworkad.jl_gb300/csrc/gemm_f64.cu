@@ -152,6 +152,10 @@ void gemm(tnad_ctx* c, int prec, char ta, char tb, int64_t M, int64_t N, int64_t
   if (prec == TNAD_PREC_TF32X3) {
     TNAD_REQUIRE(c->tc_ok, TNAD_ERR_STATE, "TF32X3 contractions need an sm_100-family GPU (tcgen05)");
     gemm_tf32x3(c, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+  } else if (prec == TNAD_PREC_FP64_TC) {
+    gemm_fp64tc(c, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, true);
+  } else if (prec == TNAD_PREC_FP64 && c->fp64_tc) {
+    gemm_fp64tc(c, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
   } else {
     gemm_f64(c, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
   }

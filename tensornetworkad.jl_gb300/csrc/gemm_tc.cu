@@ -28,6 +28,7 @@
 #include <cstring>
 #include <mutex>
 
+#include "tc_common.cuh"
 #include "tnad_internal.h"
 
 namespace tnad {
@@ -46,87 +47,10 @@ struct Cfg {
   static constexpr int KSLICE = SPLIT ? 32 : 64;  // elements per 128-byte K slice (TF32 / BF16)
 };
 
-__device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+using namespace tc;
 
-__device__ __forceinline__ uint64_t gtime() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// bounded wait: false (and *err set) after limit_ns (2 s in normal operation)
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code, uint64_t limit_ns) {
-  if (mbar_try(bar, parity)) return true;
-  uint64_t t0 = gtime();
-  while (!mbar_try(bar, parity)) {
-    if (gtime() - t0 > limit_ns) {
-      atomicExch(err, code);
-      return false;
-    }
-  }
-  return true;
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* tm, int x, int y, uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-          dst),
-      "l"(tm), "r"(x), "r"(y), "r"(bar)
-      : "memory");
-}
-
-// UMMA shared-memory descriptor: K-major operand, 128B swizzle, 8-row groups 1024 B apart.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
-  uint64_t d = 0;
-  d |= (uint64_t)((addr & 0x3FFFFu) >> 4);
-  d |= (uint64_t)1 << 16;            // leading byte offset (unused for swizzled K-major)
-  d |= (uint64_t)(1024 >> 4) << 32;  // stride byte offset
-  d |= (uint64_t)1 << 46;            // descriptor version (tcgen05)
-  d |= (uint64_t)2 << 61;            // SWIZZLE_128B
-  return d;
-}
-
-__device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
-      "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
-      : "memory");
-}
-
-__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
-      "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
-      : "memory");
-}
-
-__device__ __forceinline__ void mma_commit(uint32_t bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
-}
+// UMMA descriptor of a K-major tile with 128-byte swizzled rows (8-row groups 1024 B apart)
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) { return tc::smem_desc(addr, 1024, 2); }
 
 __device__ __forceinline__ float tf32_rn(float x) {
   uint32_t r;
@@ -351,22 +275,7 @@ __global__ void k_splitk_sum(int64_t M, int64_t N, int splits, const double* __r
   }
 }
 
-typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiledFn encode_fn() {
-  static EncodeTiledFn fn = nullptr;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = (EncodeTiledFn)p;
-  });
-  return fn;
-}
+EncodeTiledFn encode_fn() { return tensor_map_encoder(); }
 
 CUtensorMap make_map(void* base, int64_t k_pad, int64_t rows_pad, int box_rows, bool bf16) {
   CUtensorMap m;
@@ -495,6 +404,19 @@ void gemm_bf16(tnad_ctx* c, char ta, char tb, int64_t M, int64_t N, int64_t K, f
     launch_tc<128, false, float>(c, M, N, K, alpha, Ab, nullptr, Bb, nullptr, Mp, Np, Kp, beta, Cm, ldc, "gemm_bf16");
   else
     launch_tc<64, false, float>(c, M, N, K, alpha, Ab, nullptr, Bb, nullptr, Mp, Np, Kp, beta, Cm, ldc, "gemm_bf16");
+}
+
+EncodeTiledFn tensor_map_encoder() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+  });
+  return fn;
 }
 
 // Host check of the bounded-wait error flag (TNAD_ERR_TIMEOUT when a tensor-core

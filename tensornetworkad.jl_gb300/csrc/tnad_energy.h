@@ -21,6 +21,7 @@ struct EnergyTape {
   double fp_residual = 0.0, fp_tol = 1e-10, last_diff = 0.0;
   double fp_fixed_point_residual = 0.0;  // ‖f(x*) − x*‖/‖x*‖ of the aligned step (implicit adjoint)
   int fp_maxit = 200;
+  bool fp64_tc = false;  // FP64 products as tensor-core emulation (tnad_opts.fp64_tc)
   double E = 0.0;
   DevPool pool;
   double *h = nullptr, *As = nullptr, *nA = nullptr, *ap = nullptr, *a = nullptr;

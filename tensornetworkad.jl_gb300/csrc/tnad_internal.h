@@ -91,6 +91,9 @@ struct tnad_ctx {
   //     (TNAD_ERR_NOT_CONVERGED).
   // Each is cleared when used; later calls on the context run normally.
   int fault_once = 0;
+  // FP64 products (TNAD_PREC_FP64) of the current call run as gemm_fp64tc on
+  // the tensor cores instead of DFMA tiles (tnad_opts.fp64_tc; Fp64TcScope)
+  bool fp64_tc = false;
   // kernel timer (tnad_ctx_kernel_timer): events around every launch of one
   // kernel family, with the algorithmic work (flops or bytes) of each launch
   std::string ktimer;
@@ -142,6 +145,14 @@ struct KernelTimer {
   ~KernelTimer() {
     if (e1) cudaEventRecord(e1, c->stream);
   }
+};
+
+// Sets the context's FP64-product route for one call and restores it after.
+struct Fp64TcScope {
+  tnad_ctx* c;
+  bool prev;
+  Fp64TcScope(tnad_ctx* ctx, bool on) : c(ctx), prev(ctx->fp64_tc) { c->fp64_tc = on && c->tc_ok; }
+  ~Fp64TcScope() { c->fp64_tc = prev; }
 };
 
 // RAII scope over the context's workspace stack.
@@ -196,6 +207,12 @@ void gemm_tf32x3(tnad_ctx* c, char ta, char tb, int64_t M, int64_t N, int64_t K,
 // accumulation on tcgen05 tensor cores (chunks of 512 K values summed in FP64).
 void gemm_bf16(tnad_ctx* c, char ta, char tb, int64_t M, int64_t N, int64_t K, float alpha, const float* A,
                int64_t lda, const float* B, int64_t ldb, float beta, float* C, int64_t ldc);
+// Same contract, FP64-accurate (about 2^−47 of the row/column scales) from BF16
+// slices on the tcgen05 tensor cores (gemm_oz.cu); unless `always`, products
+// below a few million multiply-adds go to gemm_f64 (as fast there).
+void gemm_fp64tc(tnad_ctx* c, char ta, char tb, int64_t M, int64_t N, int64_t K, double alpha,
+                 const double* A, int64_t lda, const double* B, int64_t ldb, double beta,
+                 double* C, int64_t ldc, bool always = false);
 // Raises TNAD_ERR_TIMEOUT if a tensor-core GEMM gave up on a bounded wait (syncs).
 void check_tc_errors(tnad_ctx* c);
 void gemm(tnad_ctx* c, int prec, char ta, char tb, int64_t M, int64_t N, int64_t K, double alpha,

@@ -106,3 +106,50 @@ def test_mixed_reaches_1e8_of_oracle_Estar(tn, orc, name):
     E, g = tn.energy_and_gradient(h, tn.SquareIPEPS(A), w["chi"], 3e-8, 400, opts=tn.mixed_opts(), stats=st)
     assert abs(E - w["E_star"]) <= 1e-8, (E, w["E_star"], st)
     assert np.all(np.isfinite(g))
+
+
+def _unit_direction(shape, seed):
+    v = np.random.default_rng(seed).standard_normal(shape)
+    return v / np.linalg.norm(v)
+
+
+def test_mixed_D4_chi100_reaches_1e8_and_its_gradient_matches_a_difference_quotient(tn):
+    """The large-environment configuration at χ = 100 (enlarged corner
+    1600×1600, D = 4 N(0,1) tensor, seed 0): |E − E*| ≤ 1e-8 against the
+    oracle's converged energy (tests/golden/estar.json), and the implicit-adjoint
+    gradient along a random unit direction against a central difference
+    (step 1e-4) of mixed-path energies converged to the stop rule 1e-10."""
+    w = ESTAR["heisenberg_D4_chi100"]
+    A = tn.site_tensor(w["recipe"], w["D"], 2, w["seed"])
+    h = tn.hamiltonian(tn.Heisenberg())
+    st = {}
+    E, g = tn.energy_and_gradient(h, tn.SquareIPEPS(A), 100, 3e-8, 400, opts=tn.mixed_opts(), stats=st)
+    assert abs(E - w["E_star"]) <= 1e-8, (E, w["E_star"], st)
+    assert st["fixed_point_residual"] < 1e-5, st
+    v, step = _unit_direction(A.shape, 1), 1e-4
+    Ep = tn.energy(h, tn.SquareIPEPS(np.asfortranarray(A + step * v)), 100, 1e-10, 400, tn.mixed_opts())
+    Em = tn.energy(h, tn.SquareIPEPS(np.asfortranarray(A - step * v)), 100, 1e-10, 400, tn.mixed_opts())
+    fd = (Ep - Em) / (2 * step)
+    gv = float(np.sum(g * v))
+    assert abs(gv - fd) <= 1e-4 * abs(fd) + 2e-7, (gv, fd, st)
+
+
+def test_mixed_path_beyond_one_cta_polar_factor_chi130(tn):
+    """χ = 130 (above the 128 that the one-CTA Newton–Schulz polar factor holds):
+    the gauge alignment and the fixed-point adjoint take the multi-CTA polar
+    factor.  D = 3 uniform tensor: mixed energy against the plain FP64 path at
+    the same χ, and the gradient along a random direction against a central
+    difference of plain FP64 energies."""
+    h = tn.hamiltonian(tn.Heisenberg())
+    A = tn.site_tensor("uniform", 3, 2, 0)
+    st = {}
+    E, g = tn.energy_and_gradient(h, tn.SquareIPEPS(A), 130, 1e-10, 300, opts=tn.mixed_opts(), stats=st)
+    plain = tn.default_opts()
+    E_p = tn.energy(h, tn.SquareIPEPS(A), 130, 1e-11, 300, plain)
+    assert abs(E - E_p) <= 1e-8, (E, E_p, st)
+    v, step = _unit_direction(A.shape, 2), 1e-4
+    Ep = tn.energy(h, tn.SquareIPEPS(np.asfortranarray(A + step * v)), 130, 1e-11, 300, plain)
+    Em = tn.energy(h, tn.SquareIPEPS(np.asfortranarray(A - step * v)), 130, 1e-11, 300, plain)
+    fd = (Ep - Em) / (2 * step)
+    gv = float(np.sum(g * v))
+    assert abs(gv - fd) <= 1e-4 * abs(fd) + 2e-7, (gv, fd, st)

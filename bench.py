@@ -293,7 +293,7 @@ def run_gb300(args):
     # is bracketed as a whole: its average launch duration includes the
     # graph's gaps between rounds)
     fam = {}
-    for name in ("jacobi_round", "jacobi_round_f32", "gemm_tf32x3", "gemm_f64"):
+    for name in ("jacobi_round", "jacobi_round_f32", "gemm_tf32x3", "gemm_f64", "gemm_fp64tc"):
         kernel_timer(c, name)
         sol.device()
         fam[name] = kernel_timer_read(c)
@@ -302,6 +302,7 @@ def run_gb300(args):
     tn_n, tn_ms, tn_work = fam["gemm_tf32x3"]
     k32n, k32ms, k32work = fam["jacobi_round_f32"]
     gf_n, gf_ms, gf_work = fam["gemm_f64"]
+    oz_n, oz_ms, oz_work = fam["gemm_fp64tc"]
     # end to end through the public API with host (NumPy) arrays: every call
     # copies A and h to the device and E and dE/dA back
     sol.host()
@@ -336,6 +337,8 @@ def run_gb300(args):
     ach_fp64 = (kwork / (kms / 1e3)) / 1e12 if kms > 0 else None
     ach_tc = (tn_work / (tn_ms / 1e3)) / 1e12 if tn_ms > 0 else None
     ach_gf = (gf_work / (gf_ms / 1e3)) / 1e12 if gf_ms > 0 else None
+    ach_oz = (oz_work / (oz_ms / 1e3)) / 1e12 if oz_ms > 0 else None
+    bf16_peak = pk.get("bf16_tflops", 1900.0)
     tf32_peak = pk.get("bf16_tflops", 1900.0) / 2.0
     nA = int(np.asarray(sol.A).size)
     line = {
@@ -382,6 +385,14 @@ def run_gb300(args):
                                "launches_per_step": gf_n,
                                "avg_launch_us": round(gf_ms * 1e3 / gf_n, 3) if gf_n else None,
                                "share_of_step": round(gf_ms / 1e3 / t_dev, 4) if gf_n else None},
+        "roofline_fp64_tc": {"kernel": "k_gemm_oz (FP64-accurate products from six BF16 slices per operand on "
+                                       "tcgen05: 26 slice-pair products per FP64 product)", "bound": "tensor",
+                             "achieved_logical_fp64": round(ach_oz, 3) if ach_oz else None,
+                             "achieved_hw": round(26 * ach_oz, 3) if ach_oz else None, "peak": bf16_peak,
+                             "unit": "TFLOP/s", "frac": round(26 * ach_oz / bf16_peak, 4) if ach_oz else None,
+                             "peak_kind": f"{pk_kind} bf16 burst (MEASURED_PEAKS.json)", "launches_per_step": oz_n,
+                             "avg_launch_us": round(oz_ms * 1e3 / oz_n, 3) if oz_n else None,
+                             "share_of_step": round(oz_ms / 1e3 / t_dev, 4) if oz_n else None},
         "clocks": clk.summary(),
     }
     if plain:

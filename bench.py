@@ -684,6 +684,18 @@ def run_optimise(args):
     E_start = tn.energy(h, tn.SquareIPEPS(A0), chi, 1e-10, 400, tn.mixed_opts())
     for v in out.values():
         v["E_start"] = E_start
+    if not args.only or args.only == "mixed_device_lbfgs":
+        # the library's own L-BFGS (iterate and pairs on the device, Armijo backtracking)
+        o = tn.mixed_opts()
+        tn.energy(h, tn.SquareIPEPS(A0), chi, 3e-8, 400, o)  # warm-up
+        st = {}
+        t0 = time.perf_counter()
+        E, _ = tn.optimiseipeps(tn.SquareIPEPS(A0), h, chi, 3e-8, 400, f_tol=0.0, iterations=args.lbfgs_steps,
+                                opts=o, driver="device", stats=st)
+        dt = time.perf_counter() - t0
+        out["mixed_device_lbfgs"] = {"iterations": st["iterations"], "evaluations": st["evaluations"],
+                                     "seconds": round(dt, 2), "s_per_evaluation": round(dt / max(st["evaluations"], 1), 3),
+                                     "E_final": E, "stop_tol": 3e-8}
     line = {"metric": f"optimiseipeps: {args.lbfgs_steps} L-BFGS iterations at D=4, chi={chi} (Heisenberg)",
             "unit": "s", "higher_is_better": False, "config": {"workload": f"optimise_D4_chi{chi}", "D": 4,
                                                               "chi": chi, "lbfgs_m": 20},

@@ -169,6 +169,17 @@ int tnad_svd(tnad_ctx* ctx, const double* A, int m, int n, double* U, double* S,
    device resolves that array's address and should come before any stream
    capture.  Sizes beyond 256 return TNAD_ERR_SHAPE. */
 int tnad_svd_noalloc(const double* A, int m, int n, double* U, double* S, double* V, void* stream);
+/* ComplexF64 versions (arrays interleaved (re, im), exactly as a Julia
+   Array{ComplexF64} is laid out; host pointers).  tnad_svd_z: thin SVD of the
+   m×n A (any m, n; K = min(m, n)): U m×K, S K (real, descending), V n×K with
+   A = U·diag(S)·Vᴴ, by one-sided Jacobi with complex plane rotations; columns
+   with a zero singular value come back as zero vectors.  Replaces
+   LinearAlgebra.svd on complex input (test/svd.jl).  tnad_svd_back_z: svd_back
+   of src/trg.jl:72-105 for complex U, V, including the imaginary-diagonal term
+   of :85; dU m×K, dS K (real), dV n×K may be NULL. */
+int tnad_svd_z(tnad_ctx* ctx, const double* A, int m, int n, double* U, double* S, double* V);
+int tnad_svd_back_z(tnad_ctx* ctx, const double* U, const double* S, const double* V, int m, int n,
+                    const double* dU, const double* dS, const double* dV, double eta, double* dA);
 /* svd_back(U,S,V,dU,dS,dV; η) of src/trg.jl:72-105 (real).  dU/dS/dV may be NULL. */
 int tnad_svd_back(tnad_ctx* ctx, const double* U, const double* S, const double* V,
                   int m, int n, const double* dU, const double* dS, const double* dV,
@@ -210,6 +221,19 @@ int tnad_energy(tnad_ctx* ctx, const double* h, const double* A, int D, int s, i
                 double tol, int maxit, const tnad_opts* opts, const double* C_init,
                 const double* T_init, double* E, int* steps, double* C_out, double* T_out,
                 tnad_tape** tape);
+/* optimiseipeps(ipeps, h; χ, tol, maxit, optimargs, optimmethod = LBFGS(m)) of
+   src/variationalipeps.jl:67-75, run inside the library: L-BFGS with m correction
+   pairs on the site tensor A (D×D×D×D×s, in: the start, out: the minimiser),
+   every evaluation the energy and gradient of tnad_energy/tnad_energy_backward
+   under opts (CTMRG from :raw each time, as the reference does).  The iterate,
+   gradient and pairs stay on the device; each line-search trial returns only its
+   energy to the host.  Stops after `iterations`, when |ΔE| ≤ f_tol·|E|, when
+   max|∂E/∂A| ≤ g_tol, or when the backtracking line search finds no decrease.
+   E_out, iters_out, evals_out may be NULL.  With opts->device_ptrs, h and A are
+   device pointers. */
+int tnad_optimiseipeps(tnad_ctx* ctx, const double* h, double* A, int D, int s, int chi, double tol, int maxit,
+                       const tnad_opts* opts, int m, int iterations, double f_tol, double g_tol, double* E_out,
+                       int* iters_out, int* evals_out);
 /* dA = dE · ∂energy/∂A (Zygote.gradient of energy, src/variationalipeps.jl:71-73). */
 int tnad_energy_backward(tnad_ctx* ctx, tnad_tape* tape, double dE, double* dA);
 /* Diagnostics of an energy tape (any pointer may be NULL): CTMRG steps, FP64

@@ -80,27 +80,32 @@ def norm(a):
 
 
 def svd_back(U, S, V, dU, dS, dV, eta: float = 1e-40):
-    """Real restatement of svd_back (src/trg.jl:72-105)."""
+    """Restatement of svd_back (src/trg.jl:72-105), real or complex U, V."""
     if dU is None and dS is None and dV is None:
         return None
     S2 = S * S
     Sinv = S / (S2 + eta)
     F = S2[None, :] - S2[:, None]           # F[i,j] = s_j^2 - s_i^2   (:78)
     F = F / (F * F + eta)                    # (:79)
-    res = torch.zeros(S.shape[0], S.shape[0], dtype=S.dtype)
+    cplx = U.is_complex()
+    res = torch.zeros(S.shape[0], S.shape[0], dtype=U.dtype)
     if dU is not None:
-        J = F * (U.T @ dU)                   # (:83-84)
-        res = res + (J + J.T) * S[None, :]   # (:85) (J+J')*Diagonal(S); imag term is 0 for real
+        UdU = U.conj().T @ dU                # (:83)
+        J = F * UdU                          # (:84)
+        res = res + (J + J.conj().T) * S[None, :]   # (:85) (J+J')*Diagonal(S)
+        if cplx:                                    # (:85) + Diagonal(1im*imag(diag(UdU)) .* Sinv)
+            res = res + torch.diag(1j * torch.diagonal(UdU).imag * Sinv)
     if dV is not None:
-        K = F * (V.T @ dV)                   # (:88-89)
-        res = res + S[:, None] * (K + K.T)
+        K = F * (V.conj().T @ dV)            # (:88-89)
+        res = res + S[:, None] * (K + K.conj().T)   # (:90)
     if dS is not None:
-        res = res + torch.diag(dS)           # (:93)
-    out = U @ res @ V.T                      # (:96)
+        res = res + torch.diag(dS).to(res.dtype)    # (:93)
+    out = U @ res @ V.conj().T               # (:96)
     if dU is not None and U.shape[0] != U.shape[1]:
-        out = out + ((dU - U @ (U.T @ dU)) * Sinv[None, :]) @ V.T          # (:98-99)
+        out = out + ((dU - U @ (U.conj().T @ dU)) * Sinv[None, :]) @ V.conj().T          # (:98-99)
     if dV is not None and V.shape[0] != V.shape[1]:
-        out = out + (U * Sinv[None, :]) @ (dV.T - (dV.T @ V) @ V.T)          # (:102-103)
+        dVh = dV.conj().T
+        out = out + (U * Sinv[None, :]) @ (dVh - (dVh @ V) @ V.conj().T)                 # (:102-103)
     return out
 
 
@@ -110,7 +115,7 @@ class _SVD(torch.autograd.Function):
     @staticmethod
     def forward(ctx, A):
         U, S, Vh = torch.linalg.svd(A, full_matrices=False)
-        V = Vh.T.contiguous()
+        V = Vh.conj().T.contiguous()
         ctx.save_for_backward(U, S, V)
         ctx.set_materialize_grads(False)
         return U, S, V

@@ -170,6 +170,30 @@ def svd(A):
     return U, S, V
 
 
+def svd_complex(A):
+    """Thin SVD of a complex matrix on the GPU: (U, S, V) with A = U·diag(S)·Vᴴ."""
+    A = L.zarr(A)
+    m, n = A.shape
+    k = min(m, n)
+    U, V = np.zeros((m, k), np.complex128, order="F"), np.zeros((n, k), np.complex128, order="F")
+    S = fzeros((k,))
+    c = ctx()
+    c.check(c.lib.tnad_svd_z(c.h, L.zptr(A), m, n, L.zptr(U), ptr(S), L.zptr(V)))
+    return U, S, V
+
+
+def svd_back_complex(U, S, V, dU=None, dS=None, dV=None, eta: float = 1e-40):
+    """Complex SVD adjoint (src/trg.jl:72-105, with the imaginary-diagonal term of :85) on the GPU."""
+    U, V, S = L.zarr(U), L.zarr(V), farr(S)
+    m, n = U.shape[0], V.shape[0]
+    dA = np.zeros((m, n), np.complex128, order="F")
+    c = ctx()
+    c.check(c.lib.tnad_svd_back_z(c.h, L.zptr(U), ptr(S), L.zptr(V), m, n,
+                                  L.zptr(None if dU is None else L.zarr(dU)), ptr(None if dS is None else farr(dS)),
+                                  L.zptr(None if dV is None else L.zarr(dV)), float(eta), L.zptr(dA)))
+    return dA
+
+
 def svd_back(U, S, V, dU=None, dS=None, dV=None, eta: float = 1e-40):
     """SVD adjoint (src/trg.jl:72-105) on the GPU."""
     U, S, V = farr(U), farr(S), farr(V)
@@ -410,11 +434,28 @@ def mixed_opts(ladder_tol: float = 1e-5, fp_tol: float = 1e-9, fp_maxit: int = 2
 
 
 def optimiseipeps(ipeps: IPEPS, h, chi: int, tol: float, maxit: int, f_tol: float = 1e-6, iterations: int = 1000,
-                  m: int = 20, callback=None, opts=None):
-    """optimiseipeps (src/variationalipeps.jl:67-75): L-BFGS(m) on energy with the GPU gradient.
+                  m: int = 20, callback=None, opts=None, driver: str = "scipy", g_tol: float = 1e-10,
+                  stats: dict | None = None):
+    """optimiseipeps (src/variationalipeps.jl:67-75): L-BFGS(m) on energy with the GPU gradient;
+    returns (minimum, minimizer).
 
-    SciPy's L-BFGS-B plays Optim's LBFGS(m = 20); returns (minimum, minimizer).
+    driver="scipy": SciPy's L-BFGS-B on the host plays Optim's LBFGS(m = 20), one
+    library call per evaluation.  driver="device": the L-BFGS of the library
+    (tnad_optimiseipeps), iterate and pairs on the device, Armijo backtracking;
+    ``stats`` receives its iteration and evaluation counts.
     """
+    if driver == "device":
+        A = farr(ipeps.bulk).copy(order="F")
+        D, s = A.shape[0], A.shape[4]
+        E, it, ev = C.c_double(), C.c_int(), C.c_int()
+        o = opts or default_opts()
+        c = ctx()
+        c.check(c.lib.tnad_optimiseipeps(c.h, ptr(farr(h)), ptr(A), D, s, int(chi), float(tol), int(maxit),
+                                         C.byref(o), int(m), int(iterations), float(f_tol), float(g_tol),
+                                         C.byref(E), C.byref(it), C.byref(ev)))
+        if stats is not None:
+            stats.update(iterations=it.value, evaluations=ev.value)
+        return E.value, A
     import scipy.optimize
 
     shape = ipeps.bulk.shape

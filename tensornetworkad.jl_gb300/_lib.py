@@ -74,6 +74,8 @@ SIGNATURES = {
     "tnad_svd": (C.c_int, [VP, DP, C.c_int, C.c_int, DP, DP, DP]),
     "tnad_svd_noalloc": (C.c_int, [DP, C.c_int, C.c_int, DP, DP, DP, VP]),
     "tnad_svd_back": (C.c_int, [VP, DP, DP, DP, C.c_int, C.c_int, DP, DP, DP, C.c_double, DP]),
+    "tnad_svd_z": (C.c_int, [VP, DP, C.c_int, C.c_int, DP, DP, DP]),
+    "tnad_svd_back_z": (C.c_int, [VP, DP, DP, DP, C.c_int, C.c_int, DP, DP, DP, C.c_double, DP]),
     "tnad_ctmrgstep": (C.c_int, [VP, DP, C.c_int, C.c_int, DP, DP, DP, DP, DP]),
     "tnad_ctmrgstep_backward": (C.c_int, [VP, DP, C.c_int, C.c_int, DP, DP, DP, DP, DP, DP, DP]),
     "tnad_init_raw": (C.c_int, [VP, DP, C.c_int, C.c_int, DP, DP]),
@@ -85,6 +87,8 @@ SIGNATURES = {
     "tnad_energy": (C.c_int, [VP, DP, DP, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.POINTER(Opts), DP, DP,
                               DP, IP, DP, DP, C.POINTER(VP)]),
     "tnad_energy_backward": (C.c_int, [VP, VP, C.c_double, DP]),
+    "tnad_optimiseipeps": (C.c_int, [VP, DP, DP, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.POINTER(Opts),
+                                     C.c_int, C.c_int, C.c_double, C.c_double, DP, IP, IP]),
     "tnad_energy_stats": (C.c_int, [VP, IP, IP, IP, IP, DP, DP]),
     "tnad_energy_fixed_point_residual": (C.c_int, [VP, DP]),
     "tnad_mlp_create": (C.c_int, [VP, C.c_int, C.c_int, C.c_int, C.c_uint64, C.POINTER(VP)]),
@@ -217,6 +221,18 @@ def fptr(a) -> FP:
         return C.cast(C.c_void_p(a), FP)
     assert a.flags["F_CONTIGUOUS"] and a.dtype == np.float32
     return a.ctypes.data_as(FP)
+
+
+def zarr(x) -> np.ndarray:
+    """complex128 column-major array (interleaved re/im, Julia's ComplexF64 layout)."""
+    return np.asfortranarray(np.asarray(x, dtype=np.complex128))
+
+
+def zptr(a) -> DP:
+    if a is None:
+        return C.cast(None, DP)
+    assert a.flags["F_CONTIGUOUS"] and a.dtype == np.complex128
+    return a.ctypes.data_as(DP)
 
 
 def fzeros(shape) -> np.ndarray:

@@ -32,3 +32,36 @@ def test_optimiseipeps_reaches_reference_energy(tn, model, args, chi, tol, maxit
         if abs(best - expected) <= atol:
             break
     assert abs(best - expected) <= atol, best
+
+
+@pytest.mark.parametrize("model,args,chi,tol,maxit,f_tol,expected,atol", [CASES[0], CASES[3], CASES[5]])
+def test_device_lbfgs_reaches_reference_energy(tn, model, args, chi, tol, maxit, f_tol, expected, atol):
+    """The same cases with the library's own L-BFGS (tnad_optimiseipeps: iterate
+    and correction pairs on the device, Armijo backtracking)."""
+    h = tn.hamiltonian(getattr(tn, model)(*args))
+    opts = tn.default_opts(prec=0, solver=0, adjoint=0)
+    best = np.inf
+    for seed in (1, 2, 3):
+        x0 = np.random.default_rng(seed).standard_normal((2, 2, 2, 2, 2))
+        st = {}
+        e, x = tn.optimiseipeps(tn.SquareIPEPS(x0), h, chi, tol, maxit, f_tol=f_tol, iterations=300, opts=opts,
+                                driver="device", stats=st)
+        assert st["evaluations"] >= st["iterations"] >= 1
+        # the returned minimiser has the returned energy
+        assert abs(tn.energy(h, tn.SquareIPEPS(x), chi, tol, maxit, opts) - e) <= 1e-12 * abs(e)
+        best = min(best, e)
+        if abs(best - expected) <= atol:
+            break
+    assert abs(best - expected) <= atol, best
+
+
+def test_device_lbfgs_mixed_path_D4_lowers_the_energy(tn):
+    """Five device L-BFGS iterations at D = 4, χ = 32 on the mixed path (implicit
+    adjoint): the energy decreases monotonically from the start."""
+    h = tn.hamiltonian(tn.Heisenberg())
+    A = tn.site_tensor("normal_maxabs", 4, 2, 0)
+    E0 = tn.energy(h, tn.SquareIPEPS(A), 32, 1e-8, 400, tn.mixed_opts())
+    st = {}
+    E, _ = tn.optimiseipeps(tn.SquareIPEPS(A), h, 32, 1e-8, 400, f_tol=0.0, iterations=5, opts=tn.mixed_opts(),
+                            driver="device", stats=st)
+    assert st["iterations"] == 5 and E < E0 - 1e-3, (E, E0, st)

@@ -164,3 +164,73 @@ def test_heisenberg_readme_random_energy_range(orc):
     h = orc.hamiltonian_heisenberg()
     e = float(orc.energy(h, torch.as_tensor(orc.ipeps_uniform(2, 2, 0)), 20, 1e-6, 100))
     assert -0.7 < e < -0.3
+
+
+# ----------------------------------------------------------------- complex SVD adjoint
+def _gradient_check(f, x, eta=1e-5):
+    """test/svd.jl:6-13: f(x) − f(x − η·g) ≈ η·Σ|g|² (rtol 1e-2, atol 1e-8)."""
+    import torch
+
+    xt = torch.as_tensor(x).clone().requires_grad_(True)
+    (g,) = torch.autograd.grad(f(xt), xt)
+    dy = float(f(torch.as_tensor(x))) - float(f(torch.as_tensor(x) - eta * g))
+    dy_expect = eta * float((g.abs() ** 2).sum())
+    return abs(dy - dy_expect) <= 1e-8 + 1e-2 * abs(dy_expect)
+
+
+def _complex_losses(orc, seed):
+    import torch
+
+    def loss_u(A):
+        U, S, V = orc.svd(A)
+        H = torch.as_tensor(_herm(A.shape[0], seed))
+        psi = U[:, 0]
+        return (psi.conj() @ H @ psi).real
+
+    def loss_v(A):
+        U, S, V = orc.svd(A)
+        H = torch.as_tensor(_herm(A.shape[1], seed))
+        psi = V[:, 0]
+        return (psi.conj() @ H @ psi).real
+
+    def loss_uv(A):
+        U, S, V = orc.svd(A)
+        return (U[0, 0].conj() * V[0, 0]).real
+
+    def loss_s(A):
+        U, S, V = orc.svd(A)
+        return S.sum()
+
+    return {"U": loss_u, "V": loss_v, "UV": loss_uv, "S": loss_s}
+
+
+def _herm(n, seed):
+    rng = np.random.default_rng(seed)
+    H = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    return H + H.conj().T
+
+
+@pytest.mark.parametrize("shape", [(6, 3), (3, 6), (3, 3)])
+@pytest.mark.parametrize("which", ["U", "V", "UV", "S"])
+def test_oracle_complex_svd_adjoint_taylor(orc, shape, which):
+    """test/svd.jl:15-101 (svd grad U, V, U+V, S on complex (6,3), (3,6), (3,3))
+    on the oracle's complex restatement of svd_back."""
+    rng = np.random.default_rng(10 * shape[0] + shape[1] + 100 * ["U", "V", "UV", "S"].index(which))
+    a = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    assert _gradient_check(_complex_losses(orc, 2)[which], a)
+
+
+def test_oracle_complex_svd_adjoint_imag_diag(orc):
+    """test/svd.jl:69-86: the fixed 2×2 complex A, gradient of Re(conj(U[1,1])·V[1,1])
+    against a central difference in Re and Im of A[2,1] (atol 1e-3)."""
+    import torch
+
+    loss = _complex_losses(orc, 2)["UV"]
+    A = np.array([[-1 + 1j, 2 + 1j], [1 - 2j, 3 + 0.8j]])
+    da = np.array([[0, 0], [1, 0]], dtype=complex)
+    f = lambda x: float(loss(torch.as_tensor(x)))
+    nd = (f(A + 1e-4 * da) - f(A - 1e-4 * da)) / 2e-4 + 1j * (f(A + 1e-4j * da) - f(A - 1e-4j * da)) / 2e-4
+    At = torch.as_tensor(A).clone().requires_grad_(True)
+    (g,) = torch.autograd.grad(loss(At), At)
+    assert abs(complex(g[1, 0]) - nd) <= 1e-3
+    assert _gradient_check(loss, A)

@@ -47,7 +47,11 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--workload", default="heisenberg_D4_chi64")
-    p.add_argument("--mode", default="mixed", choices=["plain", "mixed"])
+    p.add_argument("--mode", default="learned", choices=["plain", "mixed", "learned"],
+                   help="learned (default): the mixed path started from the learned warm start, whose network "
+                        "is trained before the warm-up on environments of other seeds of the workload's recipe")
+    p.add_argument("--learned-train", dest="learned_train", type=int, default=400,
+                   help="--mode learned: training tensors (seeds 1000..)")
     p.add_argument("--no-plain", dest="no_plain", action="store_true", help="skip the plain FP64 comparison solve")
     p.add_argument("--no-cpu-baseline", dest="no_cpu_baseline", action="store_true")
     # --workload learned_D3_chi36: learned warm start against the cold start
@@ -191,6 +195,8 @@ class Solver:
             self.opts, self.tol, self.maxit = tn.default_opts(), plain_tol(w), 400
         else:
             self.opts, self.tol, self.maxit = tn.mixed_opts(), 3e-8, 400
+            if mode == "learned":
+                self.opts.warm_start = tn._lib.WARM_LEARNED
         self.A_d = torch.tensor(np.asarray(self.A).ravel(order="F"), dtype=torch.float64, device="cuda")
         self.h_d = torch.tensor(np.asarray(self.h).ravel(order="F"), dtype=torch.float64, device="cuda")
         self.g_d = torch.zeros_like(self.A_d)
@@ -205,6 +211,7 @@ class Solver:
                                   C.byref(E), C.byref(steps), tn.ptr(None), tn.ptr(None), C.byref(tp)))
         c.check(c.lib.tnad_energy_backward(c.h, tp, 1.0, tn.ptr(self.g_d.data_ptr())))
         st = self.tn.tape_stats(self.tn._lib.Tape(c, tp, "energy"))  # frees the tape
+        st["warm_status"] = int(c.lib.tnad_ctx_warm_start_status(c.h))
         return E.value, st
 
     def host(self):
@@ -251,6 +258,31 @@ def l2_flush(buf, stream):
         buf.add_(1.0)
 
 
+def train_warm_start(tn, w, args):
+    """The learned warm start of the headline mode: targets (gauge-fixed converged
+    environments) from the mixed CTMRG on --learned-train site tensors of the
+    workload's recipe with seeds 1000.. (never the workload's own seed), a
+    3-layer width-512 network trained on the GPU (3000 AdamW steps, batch 64),
+    attached to the context.  Untimed set-up; returns its description."""
+    import importlib
+
+    wl = importlib.import_module(tn.__name__ + ".learned")
+    D, s, chi = w["D"], 2, w["chi"]
+    h = tn.hamiltonian(tn.Heisenberg())
+    t0 = time.perf_counter()
+    train = [tn.site_tensor(w["recipe"], D, s, 1000 + i) for i in range(args.learned_train)]
+    samples = wl.make_samples(train, h, chi, 1e-8, 400, tn.mixed_opts(), threads=args.threads)
+    t1 = time.perf_counter()
+    X, Y = wl.stack(samples)
+    net = wl.WarmStartNet(D, s, chi, width=512, seed=1)
+    info = net.fit(X, Y, steps=3000, batch=64, lr=1e-3, weight_decay=1e-4)
+    net.attach()
+    train_warm_start.net = net  # keep it alive while attached
+    return {"train_tensors": len(samples), "train_seeds": f"1000..{999 + args.learned_train}",
+            "targets_s": round(t1 - t0, 1), "train_s": round(info["seconds"], 2),
+            "loss_std_final": round(info["loss_std"], 5), "width": 512, "layers": 3}
+
+
 def run_gb300(args):
     import torch
     import __graft_entry__ as ge
@@ -260,6 +292,9 @@ def run_gb300(args):
     dist, rank, world = dist_init(args.gpus)
     tn = ge.load_package()
     w = ESTAR[args.workload]
+    learned = None
+    if args.mode == "learned":
+        learned = train_warm_start(tn, w, args)
     sol = Solver(tn, w, args.mode)
     c = sol.c
     stream = torch.cuda.ExternalStream(c.lib.tnad_ctx_stream(c.h))
@@ -313,8 +348,25 @@ def run_gb300(args):
     t_e2e = max_over_ranks(dist, (time.perf_counter() - t1) / args.steps)
     # the plain FP64 GPU path (full Jacobi SVD each step, unrolled reverse): one
     # warm-up solve, then the mean of three timed ones
+    cold = None
+    if args.mode == "learned":
+        # the same mixed path from the :raw start (no network): one warm-up, three timed solves
+        cs = Solver(tn, w, "mixed")
+        cs.device()
+        tcs, ecs = [], []
+        for _ in range(3):
+            torch.cuda.synchronize()
+            t2 = time.perf_counter()
+            Ec, stc = cs.device()
+            torch.cuda.synchronize()
+            tcs.append(time.perf_counter() - t2)
+            ecs.append(abs(Ec - w["E_star"]))
+        cold = {"value": round(statistics.mean(tcs), 4), "unit": "s", "ctmrg_steps": stc["steps"],
+                "fp64_steps": stc["fp64_steps"], "fixedpoint_iters": stc["fp_iters"], "delta_E": max(ecs),
+                "grad_rel_diff_vs_learned": float(np.linalg.norm(cs.g_d.cpu().numpy() - sol.g_d.cpu().numpy()) /
+                                                  np.linalg.norm(cs.g_d.cpu().numpy()))}
     plain, grad_check, g_plain = None, None, None
-    if args.mode == "mixed" and not args.no_plain:
+    if args.mode in ("mixed", "learned") and not args.no_plain:
         ps = Solver(tn, w, "plain")
         ps.device()
         tps, eps_ = [], []
@@ -345,7 +397,7 @@ def run_gb300(args):
         "metric": metric_for(w),
         "value": round(t_dev, 6), "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(t_dev * 1e3, 3), "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.mode == "plain" else "tf32x3+f64",
+        "dtype": {"plain": "f64", "mixed": "tf32x3+f64"}.get(args.mode, "tf32x3+f64 (bf16 warm-start network)"),
         "data": f"synthetic: {w['recipe']} site tensor (NumPy seed {w['seed']}), symmetrised",
         "config": {"workload": args.workload, "D": sol.D, "chi": sol.chi, "phys": sol.s, "mode": args.mode,
                    "stop_tol": sol.tol, "ctmrg_steps": stats[-1]["steps"], "fp64_steps": stats[-1]["fp64_steps"],
@@ -395,6 +447,11 @@ def run_gb300(args):
                              "share_of_step": round(oz_ms / 1e3 / t_dev, 4) if oz_n else None},
         "clocks": clk.summary(),
     }
+    if learned:
+        learned["warm_start_kept"] = sum(1 for st in stats if st.get("warm_status") == 1) / len(stats)
+        line["config"]["learned_warm_start"] = learned
+    if cold:
+        line["mixed_cold_start"] = cold
     if plain:
         line["plain_fp64"] = plain
         line["speedup_vs_plain_fp64"] = round(plain["value"] / t_dev, 2)
@@ -710,7 +767,7 @@ def run_profile(args):
 
     tn = ge.load_package()
     if args.profile == "solve":
-        E, st = Solver(tn, ESTAR[args.workload], args.mode).device()
+        E, st = Solver(tn, ESTAR[args.workload], "mixed" if args.mode == "learned" else args.mode).device()
         print(f"profile solve: E={E!r} steps={st['steps']} launches={tn.ctx().launches}", flush=True)
         return
     wl = importlib.import_module(tn.__name__ + ".learned")

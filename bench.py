@@ -64,9 +64,10 @@ def parse():
     p.add_argument("--lbfgs-steps", dest="lbfgs_steps", type=int, default=20, help="optimise_* workloads")
     p.add_argument("--chi", type=int, default=0, help="optimise_* workloads: bond dimension (default 64)")
     p.add_argument("--only", default=None, help="optimise_* workloads: run one mode only")
-    p.add_argument("--profile", default=None, choices=["solve", "mlp"],
-                   help="run one untimed solve of the workload (solve) or 20 training steps of the D=3, chi=36 "
-                        "warm-start network (mlp) and exit: the command profiled by ncu")
+    p.add_argument("--profile", default=None, choices=["solve", "mlp", "gemm_fp64tc"],
+                   help="run one untimed solve of the workload (solve), 20 training steps of the D=3, chi=36 "
+                        "warm-start network (mlp), or two FP64 tensor-core products of the adjoint's shapes "
+                        "(1024^3 and 1024x96x1024, twice: gemm_fp64tc) and exit: the commands profiled by ncu")
     return p.parse_args()
 
 
@@ -769,6 +770,14 @@ def run_profile(args):
     if args.profile == "solve":
         E, st = Solver(tn, ESTAR[args.workload], "mixed" if args.mode == "learned" else args.mode).device()
         print(f"profile solve: E={E!r} steps={st['steps']} launches={tn.ctx().launches}", flush=True)
+        return
+    if args.profile == "gemm_fp64tc":
+        rng = np.random.default_rng(0)
+        A, B, B2 = rng.standard_normal((1024, 1024)), rng.standard_normal((1024, 1024)), rng.standard_normal((1024, 96))
+        for _ in range(2):
+            tn.gemm(A, B, prec=tn._lib.PREC_FP64_TC)
+            tn.gemm(A, B2, prec=tn._lib.PREC_FP64_TC)
+        print(f"profile gemm_fp64tc: 4 products, launches={tn.ctx().launches}", flush=True)
         return
     wl = importlib.import_module(tn.__name__ + ".learned")
     net = wl.WarmStartNet(3, 2, 36, width=512, seed=1)

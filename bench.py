@@ -329,7 +329,8 @@ def run_gb300(args):
     # is bracketed as a whole: its average launch duration includes the
     # graph's gaps between rounds)
     fam = {}
-    for name in ("jacobi_round", "jacobi_round_f32", "gemm_tf32x3", "gemm_f64", "gemm_fp64tc"):
+    for name in ("jacobi_round", "jacobi_round_f32", "jacobi_round_small", "eig_refine", "gemm_tf32x3", "gemm_f64",
+                 "gemm_fp64tc"):
         kernel_timer(c, name)
         sol.device()
         fam[name] = kernel_timer_read(c)
@@ -423,6 +424,15 @@ def run_gb300(args):
                              "launches_per_step": k32n, "ms_per_step": round(k32ms, 3),
                              "avg_launch_us": round(k32ms * 1e3 / k32n, 3) if k32n else None,
                              "share_of_step": round(k32ms / 1e3 / t_dev, 4) if k32n else None},
+        "eig_refine": {"what": "GEMM refinement of the FP32 eigenvectors of the symmetric corner SVDs (one bracket "
+                              "per iteration: 6 products and the grouping kernels)",
+                       "iterations_per_step": fam["eig_refine"][0], "ms_per_step": round(fam["eig_refine"][1], 3),
+                       "share_of_step": round(fam["eig_refine"][1] / 1e3 / t_dev, 4)},
+        "jacobi_round_small": {"kernel": "k_jacobi_round_cta<2, double> (FP64 rounds of the p x p Rayleigh-Ritz "
+                                         "problems of the subspace solver)",
+                               "launches_per_step": fam["jacobi_round_small"][0],
+                               "ms_per_step": round(fam["jacobi_round_small"][1], 3),
+                               "share_of_step": round(fam["jacobi_round_small"][1] / 1e3 / t_dev, 4)},
         "roofline_tensor": {"kernel": "k_gemm_tf32x3 (tcgen05 kind::tf32, 3 split products)", "bound": "tensor",
                             "achieved_logical": round(ach_tc, 3) if ach_tc else None,
                             "achieved_hw": round(3 * ach_tc, 3) if ach_tc else None,

@@ -157,6 +157,18 @@ int tnad_trg_svd(tnad_ctx* ctx, const double* t, int d1, int d2, int d3, int d4,
    U: m×n, S: n (descending), V: n×n.  Replaces LinearAlgebra.svd at
    src/trg.jl:36 and src/ctmrg.jl:136. */
 int tnad_svd(tnad_ctx* ctx, const double* A, int m, int n, double* U, double* S, double* V);
+/* SVD A = U·diag(S)·Vᵀ of a symmetric n×n matrix (the symmetrised enlarged
+   corner cpmat of src/ctmrg.jl:134-136, decomposed there by LinearAlgebra.svd),
+   through its eigendecomposition: S = |λ| descending, V the eigenvectors,
+   U = V·sign(λ).  For n ≥ 256 FP32 Jacobi sweeps are polished to FP64 accuracy
+   by a refinement made of matrix products (FP64 Jacobi sweeps where that does
+   not converge); prec = TNAD_PREC_FP64 runs those products as DFMA tiles,
+   TNAD_PREC_FP64_TC on the tensor cores.  Host pointers. */
+int tnad_svd_sym(tnad_ctx* ctx, int prec, const double* A, int n, double* U, double* S, double* V);
+/* Diagnostics of the symmetric SVDs run on this context (no reference
+   counterpart): how many took the product refinement and how many fell back
+   to FP64 Jacobi sweeps.  Either pointer may be NULL. */
+int tnad_ctx_solver_stats(const tnad_ctx* ctx, int64_t* eig_refined, int64_t* eig_fallback);
 /* Allocation-free FP64 Jacobi SVD (no counterpart in the reference): the same
    decomposition as tnad_svd for m×n matrices with n ≤ m ≤ 256, for callers that
    cannot allocate device memory (a host framework that owns all device memory

@@ -170,6 +170,30 @@ def svd(A):
     return U, S, V
 
 
+def svd_symmetric(A, tensor_cores: bool = False):
+    """SVD of a symmetric matrix (the cpmat of src/ctmrg.jl:134-136) through its
+    eigendecomposition on the GPU: (U, S, V), S = |λ| descending, U = V·sign(λ).
+    ``tensor_cores`` runs the refinement's FP64 products on the tensor cores."""
+    A = farr(A)
+    n = A.shape[0]
+    if A.shape != (n, n):
+        raise DimensionMismatch(f"svd_symmetric needs a square matrix, got {A.shape}")
+    U, S, V = fzeros((n, n)), fzeros((n,)), fzeros((n, n))
+    c = ctx()
+    prec = L.PREC_FP64_TC if tensor_cores else L.PREC_FP64
+    c.check(c.lib.tnad_svd_sym(c.h, prec, ptr(A), n, ptr(U), ptr(S), ptr(V)))
+    return U, S, V
+
+
+def solver_stats():
+    """(refined, fell_back): symmetric SVDs of this thread's context that took the
+    product refinement / fell back to FP64 Jacobi sweeps."""
+    c = ctx()
+    r, f = C.c_int64(), C.c_int64()
+    c.check(c.lib.tnad_ctx_solver_stats(c.h, C.byref(r), C.byref(f)))
+    return int(r.value), int(f.value)
+
+
 def svd_complex(A):
     """Thin SVD of a complex matrix on the GPU: (U, S, V) with A = U·diag(S)·Vᴴ."""
     A = L.zarr(A)
@@ -519,6 +543,7 @@ def magnetisation(model: Ising, beta: float, chi: int, rng: np.random.Generator 
 
 
 __all__ = [
+    "svd_symmetric", "solver_stats",
     "Ising", "TFIsing", "Heisenberg", "hamiltonian", "diaglocalhamiltonian", "model_tensor", "mag_tensor",
     "magnetisation", "magofbeta", "trg", "trg_gradient", "trg_beta", "trg_svd", "svd", "svd_back",
     "AbstractLattice", "SquareLattice", "CTMRGRuntime", "SquareCTMRGRuntime", "ctmrg", "ctmrg_gradient",

@@ -73,6 +73,8 @@ SIGNATURES = {
     "tnad_trg_svd": (C.c_int, [VP, DP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, DP, DP, IP]),
     "tnad_svd": (C.c_int, [VP, DP, C.c_int, C.c_int, DP, DP, DP]),
     "tnad_svd_noalloc": (C.c_int, [DP, C.c_int, C.c_int, DP, DP, DP, VP]),
+    "tnad_svd_sym": (C.c_int, [VP, C.c_int, DP, C.c_int, DP, DP, DP]),
+    "tnad_ctx_solver_stats": (C.c_int, [VP, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "tnad_svd_back": (C.c_int, [VP, DP, DP, DP, C.c_int, C.c_int, DP, DP, DP, C.c_double, DP]),
     "tnad_svd_z": (C.c_int, [VP, DP, C.c_int, C.c_int, DP, DP, DP]),
     "tnad_svd_back_z": (C.c_int, [VP, DP, DP, DP, C.c_int, C.c_int, DP, DP, DP, C.c_double, DP]),

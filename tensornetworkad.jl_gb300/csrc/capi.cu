@@ -205,6 +205,33 @@ extern "C" int tnad_svd(tnad_ctx* c, const double* A, int m, int n, double* U, d
   API_END(c)
 }
 
+extern "C" int tnad_svd_sym(tnad_ctx* c, int prec, const double* A, int n, double* U, double* S, double* V) {
+  API_BEGIN(c)
+  TNAD_REQUIRE(A && U && S && V && n >= 1, TNAD_ERR_ARG, "tnad_svd_sym: needs n >= 1 and non-null arrays");
+  TNAD_REQUIRE(prec == TNAD_PREC_FP64 || prec == TNAD_PREC_FP64_TC, TNAD_ERR_ARG,
+               "tnad_svd_sym: prec must be TNAD_PREC_FP64 or TNAD_PREC_FP64_TC");
+  Fp64TcScope route(c, prec == TNAD_PREC_FP64_TC);
+  WsScope scope(c);
+  const int64_t nn = (int64_t)n * n;
+  const double* dA = to_dev(c, A, nn, false);
+  double* dU = ws_d(c, nn);
+  double* dS = ws_d(c, n);
+  double* dV = ws_d(c, nn);
+  svd_jacobi(c, dA, n, n, dU, dS, dV, true, 0);
+  to_host(c, U, dU, nn, false);
+  to_host(c, S, dS, n, false);
+  to_host(c, V, dV, nn, false);
+  finish_call(c);
+  API_END(c)
+}
+
+extern "C" int tnad_ctx_solver_stats(const tnad_ctx* c, int64_t* eig_refined, int64_t* eig_fallback) {
+  if (!c) return TNAD_ERR_ARG;
+  if (eig_refined) *eig_refined = c->eig_refined;
+  if (eig_fallback) *eig_fallback = c->eig_fallback;
+  return TNAD_OK;
+}
+
 extern "C" int tnad_svd_back(tnad_ctx* c, const double* U, const double* S, const double* V, int m, int n,
                              const double* dU, const double* dS, const double* dV, double eta, double* dA) {
   API_BEGIN(c)

@@ -106,7 +106,13 @@ __device__ __forceinline__ T wsum_t(T v) {
   return v;
 }
 
-template <int R, typename T>
+// EIG = true (symmetric A, m = n, W = A·V): the rotation diagonalises the 2×2
+// block of VᵀAV instead of the Gram matrix of W, from a = v_p·w_p, b = v_q·w_q
+// and g = (v_p·w_q + v_q·w_p)/2 (the two-sided Jacobi method for eigenvalues,
+// in the one-sided storage).  Columns for eigenvalues ±λ are then never mixed,
+// as they are in the SVD form, where both have the singular value |λ|.  Its
+// stop rule is absolute: |g| ≤ tol·√|ab| + abs_eps·‖A‖_F.
+template <int R, typename T, bool EIG = false>
 __global__ void __launch_bounds__(128) k_jacobi_round_cta(T* __restrict__ W, T* __restrict__ V, int64_t m,
                                                           int64_t n, int r, int NP, double tol, double abs_eps,
                                                           const double* __restrict__ fro2, int* __restrict__ rotated) {
@@ -138,10 +144,18 @@ __global__ void __launch_bounds__(128) k_jacobi_round_cta(T* __restrict__ W, T* 
   }
 #pragma unroll
   for (int k = 0; k < R; ++k) {
-    a = fma(x[k], x[k], a);
-    b = fma(y[k], y[k], b);
-    g = fma(x[k], y[k], g);
+    if (EIG) {
+      a = fma(vx[k], x[k], a);
+      b = fma(vy[k], y[k], b);
+      g = fma(vx[k], y[k], g);
+      g = fma(vy[k], x[k], g);
+    } else {
+      a = fma(x[k], x[k], a);
+      b = fma(y[k], y[k], b);
+      g = fma(x[k], y[k], g);
+    }
   }
+  if (EIG) g *= (T)0.5;
   a = wsum_t(a);
   b = wsum_t(b);
   g = wsum_t(g);
@@ -160,9 +174,15 @@ __global__ void __launch_bounds__(128) k_jacobi_round_cta(T* __restrict__ W, T* 
     const T B = red[1][0] + red[1][1] + red[1][2] + red[1][3];
     const T G = red[2][0] + red[2][1] + red[2][2] + red[2][3];
     T cs = 1, sn = 0;
-    const T sa = sqrt(A), sb = sqrt(B);
-    if (G != (T)0 && A != (T)0 && B != (T)0 &&
-        fabs(G) > (T)tol * sa * sb + (T)abs_eps * sqrt((T)fro2[0]) * (sa + sb)) {
+    bool do_rot;
+    if (EIG) {
+      do_rot = G != (T)0 && fabs(G) > (T)tol * sqrt(fabs(A * B)) + (T)abs_eps * sqrt((T)fro2[0]);
+    } else {
+      const T sa = sqrt(A), sb = sqrt(B);
+      do_rot = G != (T)0 && A != (T)0 && B != (T)0 &&
+               fabs(G) > (T)tol * sa * sb + (T)abs_eps * sqrt((T)fro2[0]) * (sa + sb);
+    }
+    if (do_rot) {
       const T zeta = (B - A) / ((T)2 * G);
       const T big = sizeof(T) == 8 ? (T)1e150 : (T)1e18;
       const T t = fabs(zeta) > big ? (T)0.5 / zeta : copysign((T)1, zeta) / (fabs(zeta) + sqrt((T)1 + zeta * zeta));
@@ -195,25 +215,25 @@ __global__ void __launch_bounds__(128) k_jacobi_round_cta(T* __restrict__ W, T* 
 }
 
 // one round over all column pairs (T = double or float)
-template <typename T>
+template <typename T, bool EIG = false>
 void jacobi_round_launch(tnad_ctx* c, T* W, T* V, int64_t m, int64_t n, int r, int NP, double tol, double ae,
                          const double* fro2, int* flag) {
   const unsigned np2 = (unsigned)(NP / 2);
   if (m <= 256)
-    k_jacobi_round_cta<2, T><<<np2, 128, 0, c->stream>>>(W, V, m, n, r, NP, tol, ae, fro2, flag);
+    k_jacobi_round_cta<2, T, EIG><<<np2, 128, 0, c->stream>>>(W, V, m, n, r, NP, tol, ae, fro2, flag);
   else if (m <= 512)
-    k_jacobi_round_cta<4, T><<<np2, 128, 0, c->stream>>>(W, V, m, n, r, NP, tol, ae, fro2, flag);
+    k_jacobi_round_cta<4, T, EIG><<<np2, 128, 0, c->stream>>>(W, V, m, n, r, NP, tol, ae, fro2, flag);
   else if (m <= 1024)
-    k_jacobi_round_cta<8, T><<<np2, 128, 0, c->stream>>>(W, V, m, n, r, NP, tol, ae, fro2, flag);
+    k_jacobi_round_cta<8, T, EIG><<<np2, 128, 0, c->stream>>>(W, V, m, n, r, NP, tol, ae, fro2, flag);
   else
-    k_jacobi_round_cta<16, T><<<np2, 128, 0, c->stream>>>(W, V, m, n, r, NP, tol, ae, fro2, flag);
+    k_jacobi_round_cta<16, T, EIG><<<np2, 128, 0, c->stream>>>(W, V, m, n, r, NP, tol, ae, fro2, flag);
 }
 
 // One Jacobi sweep (flag reset + the NP−1 rounds) recorded once as a CUDA
 // graph and replayed for every sweep: the rounds are short kernels whose
 // launch cost is comparable to their run time.  Very small matrices are
 // launched directly.
-template <typename T>
+template <typename T, bool EIG = false>
 struct SweepGraph {
   cudaGraphExec_t exec = nullptr;
   double ae_ = -1.0;
@@ -226,7 +246,7 @@ struct SweepGraph {
       TNAD_CK(cudaMemsetAsync(flag, 0, sizeof(int), c->stream));
       for (int r = 0; r < NP - 1; ++r) {
         KernelTimer kt(c, family, round_flops);
-        jacobi_round_launch<T>(c, W, V, m, n, r, NP, tol, ae, fro2, flag);
+        jacobi_round_launch<T, EIG>(c, W, V, m, n, r, NP, tol, ae, fro2, flag);
       }
     } else {
       if (exec && ae != ae_) {
@@ -238,7 +258,7 @@ struct SweepGraph {
         TNAD_CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
         cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int), c->stream);
         for (int r = 0; r < NP - 1 && e == cudaSuccess; ++r) {
-          jacobi_round_launch<T>(c, W, V, m, n, r, NP, tol, ae, fro2, flag);
+          jacobi_round_launch<T, EIG>(c, W, V, m, n, r, NP, tol, ae, fro2, flag);
           e = cudaGetLastError();
         }
         const cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
@@ -434,6 +454,36 @@ __global__ void k_complete_col(double* __restrict__ U, int64_t m, int64_t k, dou
   for (int64_t i = threadIdx.x; i < m; i += blockDim.x) U[i + k * m] = x[i] / nrm;
 }
 
+// rank[j] = #{i : |λ_i| > |λ_j| or (= and i < j)}: descending |λ|
+__global__ void k_eig_rank(const double* __restrict__ lam, int64_t n, int* __restrict__ rank) {
+  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const double a = fabs(lam[j]);
+  int r = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    const double b = fabs(lam[i]);
+    r += (b > a || (b == a && i < j)) ? 1 : 0;
+  }
+  rank[j] = r;
+}
+
+// SVD of a symmetric A from its eigendecomposition A = X·diag(λ)·Xᵀ:
+// S[r] = |λ_j|, V[:, r] = X[:, j], U[:, r] = sign(λ_j)·X[:, j] with r = rank[j]
+__global__ void k_scatter_eig(const double* __restrict__ X, const double* __restrict__ lam,
+                              const int* __restrict__ rank, int64_t n, double* __restrict__ U, double* __restrict__ S,
+                              double* __restrict__ V) {
+  const int64_t j = blockIdx.y;
+  const int64_t r = rank[j];
+  const double l = lam[j];
+  const double sg = l < 0.0 ? -1.0 : 1.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double x = X[i + j * n];
+    V[i + r * n] = x;
+    U[i + r * n] = sg * x;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) S[r] = fabs(l);
+}
+
 void svd_jacobi(tnad_ctx* c, const double* A, int64_t m, int64_t n, double* U, double* S, double* V,
                 bool symmetric, int rel_sweeps) {
   TNAD_REQUIRE(m >= n && n >= 1, TNAD_ERR_SHAPE, "svd_jacobi: needs m >= n >= 1");
@@ -470,19 +520,28 @@ void svd_jacobi(tnad_ctx* c, const double* A, int64_t m, int64_t n, double* U, d
   if (symmetric && n >= kPrecondMinN && m <= 2048 && !converged) {
     // FP32 preconditioning: Jacobi sweeps on a float copy (the FP32 pipe is
     // much wider than the FP64 one) until rotations stop at FP32 accuracy; the
-    // accumulated V32 is re-orthogonalised in FP64 (Newton–Schulz) and the FP64
-    // sweeps below start from W = A·V, whose columns are then orthogonal to
-    // ~1e-5: the FP64 phase needs a few sweeps instead of ~20.
+    // accumulated V32 is re-orthogonalised in FP64 (Newton–Schulz).  Then
+    // either the GEMM refinement of eig_refine.cu brings V to FP64 accuracy
+    // (the sweeps then use the eigenvalue rule, so that ±λ pairs come out as
+    // eigenvectors), or the FP64 sweeps below start from W = A·V, whose
+    // columns are then orthogonal to ~1e-5: a few sweeps instead of ~20.
+    const bool refine = c->eig_refine && m == n && n <= 2048;
     float* W32 = ws_f(c, m * n);
     float* V32 = ws_f(c, n * n);
     k_to_float<<<(int)std::min<int64_t>((m * n + 255) / 256, 4096), 256, 0, c->stream>>>(A, m * n, W32);
     k_eye_f<<<(int)nb_nn, 256, 0, c->stream>>>(V32, n);
     count_launch(c, 2);
-    const double tol32 = 4.0 * std::sqrt((double)m) * FLT_EPSILON, ae32 = 2.0 * FLT_EPSILON;
+    // eigenvalue rule: rotate while |v_pᵀAv_q| > 2ε₃₂‖A‖_F (the FP32 floor);
+    // SVD rule: relative orthogonality 4√m·ε₃₂ of the columns of W
+    const double tol32 = refine ? 0.0 : 4.0 * std::sqrt((double)m) * FLT_EPSILON, ae32 = 2.0 * FLT_EPSILON;
     SweepGraph<float> sweep32;
+    SweepGraph<float, true> sweep32e;
     const double round_flops = (double)(n / 2) * (12.0 * (double)m + 6.0 * (double)n);
     for (int sweep = 0; sweep < kMaxSweeps32; ++sweep) {
-      sweep32.run(c, "jacobi_round_f32", W32, V32, m, n, NP, tol32, ae32, fro2, flag, round_flops);
+      if (refine)
+        sweep32e.run(c, "jacobi_round_f32", W32, V32, m, n, NP, tol32, ae32, fro2, flag, round_flops);
+      else
+        sweep32.run(c, "jacobi_round_f32", W32, V32, m, n, NP, tol32, ae32, fro2, flag, round_flops);
       TNAD_CK(cudaMemcpyAsync(c->h_flag, flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
       TNAD_CK(cudaStreamSynchronize(c->stream));
       if (trace) std::fprintf(stderr, "[tnad trace] svd n=%lld fp32 sweep %d rotations %d\n", (long long)n, sweep, c->h_flag[0]);
@@ -504,6 +563,21 @@ void svd_jacobi(tnad_ctx* c, const double* A, int64_t m, int64_t n, double* U, d
       copy_d2d(c, V2, Vw, n * n);
       gemm(c, pr, 'N', 'N', n, n, n, -0.5, Vw, n, G, n, 1.5, V2, n);
       copy_d2d(c, Vw, V2, n * n);
+    }
+    if (refine) {
+      // V2 becomes the refined eigenvectors; Vw stays as the sweeps' start
+      double* lam = ws_d(c, n);
+      copy_d2d(c, V2, Vw, n * n);
+      if (eig_refine(c, A, n, V2, lam, fro2)) {
+        ++c->eig_refined;
+        k_eig_rank<<<(int)((n + 255) / 256), 256, 0, c->stream>>>(lam, n, rank);
+        dim3 g((unsigned)std::min<int64_t>((n + 255) / 256, 16), (unsigned)n);
+        k_scatter_eig<<<g, 256, 0, c->stream>>>(V2, lam, rank, n, U, S, V);
+        count_launch(c, 2);
+        check_launch(c, "svd_scatter_eig");
+        return;
+      }
+      ++c->eig_fallback;
     }
     gemm_f64(c, 'N', 'N', m, n, n, 1.0, A, m, Vw, n, 0.0, W, m);
   }

@@ -94,6 +94,12 @@ struct tnad_ctx {
   // FP64 products (TNAD_PREC_FP64) of the current call run as gemm_fp64tc on
   // the tensor cores instead of DFMA tiles (tnad_opts.fp64_tc; Fp64TcScope)
   bool fp64_tc = false;
+  // Symmetric SVDs of n ≥ 256 polish their FP32 Jacobi result by the GEMM
+  // refinement of eig_refine.cu (false: FP64 Jacobi sweeps, set by
+  // TNAD_EIG_POLISH=jacobi in the environment when the context is created),
+  // and how often that refinement was taken / fell back to the sweeps
+  bool eig_refine = true;
+  int64_t eig_refined = 0, eig_fallback = 0;
   // kernel timer (tnad_ctx_kernel_timer): events around every launch of one
   // kernel family, with the algorithmic work (flops or bytes) of each launch
   std::string ktimer;
@@ -235,6 +241,14 @@ Ten contract_shape(const Ten& A, const char* la, const Ten& B, const char* lb, c
 // √s of them is differentiated, as in TRG; 0 gives LAPACK-level accuracy).
 void svd_jacobi(tnad_ctx* c, const double* A, int64_t m, int64_t n, double* U, double* S,
                 double* V, bool symmetric, int rel_sweeps = 20);
+// Refines X (n×n, nearly orthonormal approximate eigenvectors of the symmetric
+// A, n ≤ 2048) to FP64 accuracy by matrix products; lam gets the eigenvalues
+// (column order of X).  fro2: ‖A‖²_F on the device.  false: no convergence
+// (X is then unusable and the caller falls back to Jacobi sweeps).
+bool eig_refine(tnad_ctx* c, const double* A, int64_t n, double* X, double* lam, const double* fro2);
+// The same refinement started from X = I for a small, nearly diagonal symmetric
+// p×p matrix; W, lam sorted by |λ| descending.  false: not converged.
+bool eigh_refine_small(tnad_ctx* c, const double* H, int64_t p, double* W, double* lam);
 // Symmetric eigendecomposition of a small p×p matrix (p ≤ 256) by cyclic Jacobi in
 // one CTA: A = W·diag(lam)·Wᵀ, sorted by |lam| descending.
 void eigh_small(tnad_ctx* c, const double* A, int64_t p, double* W, double* lam);

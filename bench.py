@@ -170,6 +170,8 @@ FP64_NOMINAL_TFLOPS = 1.25  # GB300 FP64 (no measured FP64 figure exists for thi
 # at n = 1024 (16 805 888 + 0 bytes; ncu flushes the caches between its passes),
 # from one ncu capture of that kernel on this workload
 JACOBI_ROUND_TRAFFIC_BYTES = 16805888
+# GB300 FP32 (CUDA-core FMA) rate: 152 SMs × 128 FMA/clock × 2 flops × 2.07 GHz
+FP32_NOMINAL_TFLOPS = 80.5
 
 
 def peaks():
@@ -335,11 +337,6 @@ def run_gb300(args):
         sol.device()
         fam[name] = kernel_timer_read(c)
     kernel_timer(c, "")
-    kn, kms, kwork = fam["jacobi_round"]
-    tn_n, tn_ms, tn_work = fam["gemm_tf32x3"]
-    k32n, k32ms, k32work = fam["jacobi_round_f32"]
-    gf_n, gf_ms, gf_work = fam["gemm_f64"]
-    oz_n, oz_ms, oz_work = fam["gemm_fp64tc"]
     # end to end through the public API with host (NumPy) arrays: every call
     # copies A and h to the device and E and dE/dA back
     sol.host()
@@ -387,13 +384,41 @@ def run_gb300(args):
     if rank != 0:
         return
     pk, pk_kind = peaks()
-    rounds = kn
-    ach_fp64 = (kwork / (kms / 1e3)) / 1e12 if kms > 0 else None
-    ach_tc = (tn_work / (tn_ms / 1e3)) / 1e12 if tn_ms > 0 else None
-    ach_gf = (gf_work / (gf_ms / 1e3)) / 1e12 if gf_ms > 0 else None
-    ach_oz = (oz_work / (oz_ms / 1e3)) / 1e12 if oz_ms > 0 else None
     bf16_peak = pk.get("bf16_tflops", 1900.0)
-    tf32_peak = pk.get("bf16_tflops", 1900.0) / 2.0
+    nominal = "nominal (no measured figure for this pipe in MEASURED_PEAKS.json)"
+    # kernel families timed live (CUDA events on the library stream): the
+    # algorithmic work of every launch, its hardware multiple (tensor-core
+    # emulations issue several products per logical one) and the peak it is
+    # measured against
+    FAM = {
+        "gemm_fp64tc": ("k_gemm_oz + slicing (FP64-accurate products from six BF16 slices per operand on tcgen05: "
+                        "26 slice-pair products per FP64 product)", "tensor", 26.0, bf16_peak,
+                        f"{pk_kind} bf16 burst (MEASURED_PEAKS.json)"),
+        "gemm_f64": ("k_gemm_f64 / k_gemv (register-tiled DFMA GEMM, matrix-vector products)", "fp64", 1.0,
+                     FP64_NOMINAL_TFLOPS, nominal),
+        "jacobi_round_f32": ("k_jacobi_block<EIG, 64> (FP32 Jacobi sweeps of the 1024x1024 corner's symmetric SVD, "
+                             "eigenvalue rule, block rounds of 4 columns)", "fp32", 1.0, FP32_NOMINAL_TFLOPS, nominal),
+        "jacobi_round_small": ("k_jacobi_round_cta<2, double> (FP64 rounds of the p x p Rayleigh-Ritz problems of the "
+                               "subspace solver)", "fp64", 1.0, FP64_NOMINAL_TFLOPS, nominal),
+        "jacobi_round": ("k_jacobi_round_cta<8, double> (FP64 sweeps of the corner SVD where the refinement falls "
+                         "back)", "fp64", 1.0, FP64_NOMINAL_TFLOPS, nominal),
+        "gemm_tf32x3": ("k_gemm_tf32x3 (tcgen05 kind::tf32, 3 split products)", "tensor", 3.0, bf16_peak / 2.0,
+                        f"{pk_kind} bf16 burst / 2 (dense TF32 rate)"),
+    }
+    families = {}
+    for name, (desc, bound, hw, peak, kind) in FAM.items():
+        fn, fms, fwork = fam[name]
+        ach = (fwork / (fms / 1e3)) / 1e12 if fms > 0 else None
+        families[name] = {"kernel": desc, "bound": bound,
+                          "achieved_logical": round(ach, 4) if ach else None,
+                          "achieved": round(hw * ach, 4) if ach else None, "peak": round(peak, 2),
+                          "unit": "TFLOP/s", "frac": round(hw * ach / peak, 4) if ach else None, "peak_kind": kind,
+                          "launches_per_step": fn, "ms_per_step": round(fms, 3),
+                          "avg_launch_us": round(fms * 1e3 / fn, 3) if fn else None,
+                          "share_of_step": round(fms / 1e3 / t_dev, 4)}
+    top = max(families, key=lambda k: families[k]["share_of_step"])
+    roofline = dict(families[top], family=top,
+                    traffic=JACOBI_ROUND_TRAFFIC_BYTES if top == "jacobi_round" else None)
     nA = int(np.asarray(sol.A).size)
     line = {
         "metric": metric_for(w),
@@ -411,51 +436,12 @@ def run_gb300(args):
         "e2e": {"value": round(t_e2e, 6), "unit": "s", "h2d_bytes_per_step": 8 * (nA + 16),
                 "d2h_bytes_per_step": 8 * (nA + 1)},
         "gpu_launches": int(launches),
-        "roofline": {"kernel": "k_jacobi_round_cta<8, double> (FP64 one-sided Jacobi round, polishing sweeps of "
-                               "the full SVD of the 1024x1024 corner for the implicit adjoint)",
-                     "bound": "fp64", "achieved": round(ach_fp64, 4) if ach_fp64 else None,
-                     "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
-                     "frac": round(ach_fp64 / FP64_NOMINAL_TFLOPS, 4) if ach_fp64 else None,
-                     "peak_kind": "nominal (no FP64 figure in MEASURED_PEAKS.json)",
-                     "traffic": JACOBI_ROUND_TRAFFIC_BYTES, "launches_per_step": round(rounds, 1),
-                     "avg_launch_us": round(kms * 1e3 / kn, 3) if kn else None,
-                     "share_of_step": round(kms / 1e3 / t_dev, 4) if kn else None},
-        "jacobi_round_f32": {"kernel": "k_jacobi_round_cta<8, float> (FP32 preconditioning sweeps of the same SVD)",
-                             "launches_per_step": k32n, "ms_per_step": round(k32ms, 3),
-                             "avg_launch_us": round(k32ms * 1e3 / k32n, 3) if k32n else None,
-                             "share_of_step": round(k32ms / 1e3 / t_dev, 4) if k32n else None},
+        "roofline": roofline,
         "eig_refine": {"what": "GEMM refinement of the FP32 eigenvectors of the symmetric corner SVDs (one bracket "
                               "per iteration: 6 products and the grouping kernels)",
                        "iterations_per_step": fam["eig_refine"][0], "ms_per_step": round(fam["eig_refine"][1], 3),
                        "share_of_step": round(fam["eig_refine"][1] / 1e3 / t_dev, 4)},
-        "jacobi_round_small": {"kernel": "k_jacobi_round_cta<2, double> (FP64 rounds of the p x p Rayleigh-Ritz "
-                                         "problems of the subspace solver)",
-                               "launches_per_step": fam["jacobi_round_small"][0],
-                               "ms_per_step": round(fam["jacobi_round_small"][1], 3),
-                               "share_of_step": round(fam["jacobi_round_small"][1] / 1e3 / t_dev, 4)},
-        "roofline_tensor": {"kernel": "k_gemm_tf32x3 (tcgen05 kind::tf32, 3 split products)", "bound": "tensor",
-                            "achieved_logical": round(ach_tc, 3) if ach_tc else None,
-                            "achieved_hw": round(3 * ach_tc, 3) if ach_tc else None,
-                            "peak": tf32_peak, "unit": "TFLOP/s",
-                            "frac": round(3 * ach_tc / tf32_peak, 4) if ach_tc else None,
-                            "peak_kind": f"{pk_kind} bf16 burst / 2 (dense TF32 rate)",
-                            "launches_per_step": tn_n, "avg_launch_us": round(tn_ms * 1e3 / tn_n, 3) if tn_n else None,
-                            "share_of_step": round(tn_ms / 1e3 / t_dev, 4) if tn_n else None},
-        "roofline_fp64_gemm": {"kernel": "k_gemm_f64 (register-tiled DFMA GEMM)", "bound": "fp64",
-                               "achieved": round(ach_gf, 4) if ach_gf else None, "peak": FP64_NOMINAL_TFLOPS,
-                               "unit": "TFLOP/s", "frac": round(ach_gf / FP64_NOMINAL_TFLOPS, 4) if ach_gf else None,
-                               "peak_kind": "nominal (no FP64 figure in MEASURED_PEAKS.json)",
-                               "launches_per_step": gf_n,
-                               "avg_launch_us": round(gf_ms * 1e3 / gf_n, 3) if gf_n else None,
-                               "share_of_step": round(gf_ms / 1e3 / t_dev, 4) if gf_n else None},
-        "roofline_fp64_tc": {"kernel": "k_gemm_oz (FP64-accurate products from six BF16 slices per operand on "
-                                       "tcgen05: 26 slice-pair products per FP64 product)", "bound": "tensor",
-                             "achieved_logical_fp64": round(ach_oz, 3) if ach_oz else None,
-                             "achieved_hw": round(26 * ach_oz, 3) if ach_oz else None, "peak": bf16_peak,
-                             "unit": "TFLOP/s", "frac": round(26 * ach_oz / bf16_peak, 4) if ach_oz else None,
-                             "peak_kind": f"{pk_kind} bf16 burst (MEASURED_PEAKS.json)", "launches_per_step": oz_n,
-                             "avg_launch_us": round(oz_ms * 1e3 / oz_n, 3) if oz_n else None,
-                             "share_of_step": round(oz_ms / 1e3 / t_dev, 4) if oz_n else None},
+        "kernel_families": families,
         "clocks": clk.summary(),
     }
     if learned:

@@ -119,6 +119,7 @@ extern "C" int tnad_ctx_create(tnad_ctx** out, int device) {
     TNAD_CK(cudaMallocHost(&c->h_flag, 64 * sizeof(int)));
     TNAD_CK(cudaMemsetAsync(c->d_flag, 0, 64 * sizeof(int), c->stream));
     if (const char* f = std::getenv("TNAD_EIG_POLISH")) c->eig_refine = std::strcmp(f, "jacobi") != 0;
+    if (const char* f = std::getenv("TNAD_JACOBI_BLOCKS")) c->jacobi_blocks = std::strcmp(f, "0") != 0;
     if (const char* f = std::getenv("TNAD_TEST_FAULT")) {
       if (!std::strcmp(f, "tc_withhold")) c->fault_once = kFaultTcWithhold;
       if (!std::strcmp(f, "jacobi_cap")) c->fault_once = kFaultJacobiCap;

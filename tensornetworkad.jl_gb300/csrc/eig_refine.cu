@@ -39,10 +39,11 @@ namespace tnad {
 
 namespace {
 
-constexpr int kMaxIt = 6;
+constexpr int kMaxIt = 8;
 constexpr int kMaxGroup = 64;
 constexpr double kEta = 0.05;
 constexpr int kMaxN = 2048;  // one CTA of 1024 threads scans the sorted order
+constexpr double kMaxStartOff = 1e-4;  // max|S_ij|/‖A‖_F of a usable start (FP32 Jacobi: ~1e-6)
 
 __device__ __forceinline__ double warp_max(double v) {
 #pragma unroll
@@ -71,10 +72,15 @@ __global__ void k_ref_colstats(const double* __restrict__ S, const double* __res
   const double* s = S + (int64_t)j * n;
   const double* g = G + (int64_t)j * n;
   double mo = 0.0, mr = 0.0;
+  bool bad = false;
   for (int i = lane; i < n; i += 32) {
-    mr = fmax(mr, fabs((i == j ? 1.0 : 0.0) - g[i]));
-    if (i != j) mo = fmax(mo, fabs(s[i]));
+    const double si = s[i], gi = g[i];
+    bad |= !isfinite(si) || !isfinite(gi);
+    mr = fmax(mr, fabs((i == j ? 1.0 : 0.0) - gi));
+    if (i != j) mo = fmax(mo, fabs(si));
   }
+  // fmax drops NaN operands: a non-finite entry is reported as an infinite maximum
+  if (__any_sync(0xffffffffu, bad)) mo = mr = INFINITY;
   mo = warp_max(mo);
   mr = warp_max(mr);
   if (lane == 0) {
@@ -472,39 +478,6 @@ __global__ void k_ref_coldots(const double* __restrict__ X, const double* __rest
 
 int nblk(int64_t n, int t = 256) { return (int)std::min<int64_t>((n + t - 1) / t, 4096); }
 
-__global__ void k_ref_eye(double* __restrict__ X, int n) {
-  const int64_t nn = (int64_t)n * n;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nn; e += (int64_t)gridDim.x * blockDim.x)
-    X[e] = (e % n == e / n) ? 1.0 : 0.0;
-}
-
-// W[:, r] = X[:, j], lam_out[r] = lam[j] with r the rank of |λ_j| (descending,
-// ties by index); one CTA per column j
-__global__ void k_ref_sort_abs(const double* __restrict__ X, const double* __restrict__ lam, int n,
-                               double* __restrict__ W, double* __restrict__ lam_out) {
-  const int j = blockIdx.x;
-  __shared__ int rank_sh;
-  const double a = fabs(lam[j]);
-  int r = 0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    const double b = fabs(lam[i]);
-    r += (b > a || (b == a && i < j)) ? 1 : 0;
-  }
-  for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
-  __shared__ int part[8];
-  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = r;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int t = 0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += part[w];
-    rank_sh = t;
-    lam_out[t] = lam[j];
-  }
-  __syncthreads();
-  const int64_t rr = rank_sh;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) W[i + rr * n] = X[i + (int64_t)j * n];
-}
-
 }  // namespace
 
 bool eig_refine(tnad_ctx* c, const double* A, int64_t n64, double* X, double* lam, const double* fro2) {
@@ -542,6 +515,7 @@ bool eig_refine(tnad_ctx* c, const double* A, int64_t n64, double* X, double* la
   int* si = g_qoff + n;  // 4 ints
   const int64_t col_threads = (int64_t)n * 32;
   bool done = false;
+  double prev_off = 0.0;
   for (int it = 0; it < kMaxIt && !done; ++it) {
     KernelTimer kt(c, "eig_refine", 6.0 * 2.0 * (double)nn * n);
     gemm(c, TNAD_PREC_FP64, 'N', 'N', n, n, n, 1.0, A, n, X, n, 0.0, AX, n);
@@ -564,7 +538,11 @@ bool eig_refine(tnad_ctx* c, const double* A, int64_t n64, double* X, double* la
     if (std::getenv("TNAD_TRACE"))
       std::fprintf(stderr, "[tnad trace] eig_refine n=%d it %d off %.2e orth %.2e groups %d (max %d, cols %d)\n", n, it,
                    hd[0], hd[1], ngroups, maxgroup, hs[2]);
+    // not an approximate eigendecomposition (the first measurement), growing
+    // errors, non-finite entries or a group too large for one CTA: give up
     if (!std::isfinite(hd[0]) || !std::isfinite(hd[1]) || maxgroup > kMaxGroup) return false;
+    if ((it == 0 && hd[0] > kMaxStartOff) || (it > 0 && hd[0] > 4.0 * prev_off)) return false;
+    prev_off = hd[0];
     done = it >= 1 && hd[0] <= 1e-10 && hd[1] <= 1e-8 && ngroups == 0;
     if (ngroups > 0) {
       // Rayleigh–Ritz inside the groups; S, G and X follow the block rotation
@@ -596,32 +574,6 @@ bool eig_refine(tnad_ctx* c, const double* A, int64_t n64, double* X, double* la
   k_ref_coldots<<<nblk(col_threads), 256, 0, c->stream>>>(X, AX, n, lam);
   count_launch(c);
   check_launch(c, "eig_refine_lam");
-  return true;
-}
-
-// Eigendecomposition H = W·diag(lam)·Wᵀ of a small symmetric p×p matrix that is
-// already nearly diagonal (the Rayleigh–Ritz matrix of a subspace iteration
-// whose basis carries the previous Ritz vectors): the refinement above started
-// from X = I, then sorted by |λ| descending.  false: not converged (W, lam
-// untouched; the caller uses a Jacobi solver instead).
-bool eigh_refine_small(tnad_ctx* c, const double* H, int64_t p, double* W, double* lam) {
-  if (!c->eig_refine || p < 2 || p > kMaxN) return false;
-  WsScope scope(c);
-  const int n = (int)p;
-  double* X = ws_d(c, p * p);
-  double* l = ws_d(c, p);
-  double* fro2 = ws_d(c, 1);
-  k_ref_eye<<<nblk(p * p), 256, 0, c->stream>>>(X, n);
-  count_launch(c);
-  sumsq_dev(c, H, p * p, fro2);
-  if (!eig_refine(c, H, p, X, l, fro2)) {
-    ++c->eig_fallback;
-    return false;
-  }
-  ++c->eig_refined;
-  k_ref_sort_abs<<<n, 256, 0, c->stream>>>(X, l, n, W, lam);
-  count_launch(c);
-  check_launch(c, "eigh_refine_small");
   return true;
 }
 

@@ -98,6 +98,65 @@ __global__ void k_splitk_reduce(int64_t M, int64_t N, int ks, const double* __re
   }
 }
 
+// Matrix-vector products (N = 1), the Gram–Schmidt steps of GMRES: a tiled
+// GEMM would compute whole 32×32 tiles for one useful column.
+// y(M) = alpha·A·x + beta·y with A M×K (lda), x K values (stride incx), K small:
+// one thread per row, coalesced over the rows of A.
+__global__ void k_gemv_n(int64_t M, int64_t K, double alpha, const double* __restrict__ A, int64_t lda,
+                         const double* __restrict__ x, int64_t incx, double beta, double* __restrict__ y) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < M; i += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int64_t k = 0; k < K; ++k) s = fma(A[i + k * lda], x[k * incx], s);
+    const double v = alpha * s;
+    y[i] = beta == 0.0 ? v : v + beta * y[i];
+  }
+}
+
+// part[chunk, i] = Σ_{k in chunk} A[k + i·lda]·x[k] for the M ≤ 32 columns of
+// A (K×M, lda): y = Aᵀx split over K chunks, threads strided over k (coalesced),
+// a fixed-order block reduction per column.
+constexpr int kGemvMaxM = 32;
+__global__ void __launch_bounds__(256) k_gemv_t_part(int64_t M, int64_t K, int64_t kchunk,
+                                                     const double* __restrict__ A, int64_t lda,
+                                                     const double* __restrict__ x, int64_t incx,
+                                                     double* __restrict__ part) {
+  __shared__ double red[8][kGemvMaxM];
+  const int64_t k0 = (int64_t)blockIdx.x * kchunk, k1 = min(K, k0 + kchunk);
+  double acc[kGemvMaxM];
+#pragma unroll
+  for (int i = 0; i < kGemvMaxM; ++i) acc[i] = 0.0;
+  for (int64_t k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+    const double xv = x[k * incx];
+#pragma unroll
+    for (int i = 0; i < kGemvMaxM; ++i)
+      if (i < M) acc[i] = fma(A[k + i * lda], xv, acc[i]);
+  }
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+  for (int i = 0; i < kGemvMaxM; ++i) {
+    double v = acc[i];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[w][i] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < M) {
+    double s = 0.0;
+    for (int ww = 0; ww < 8; ++ww) s += red[ww][threadIdx.x];
+    part[blockIdx.x * M + threadIdx.x] = s;
+  }
+}
+
+// y[i] = alpha·Σ_chunk part[chunk, i] + beta·y[i] (fixed order)
+__global__ void k_gemv_t_sum(int64_t M, int nchunk, const double* __restrict__ part, double alpha, double beta,
+                             double* __restrict__ y) {
+  const int64_t i = threadIdx.x;
+  if (i >= M) return;
+  double s = 0.0;
+  for (int z = 0; z < nchunk; ++z) s += part[z * M + i];
+  const double v = alpha * s;
+  y[i] = beta == 0.0 ? v : v + beta * y[i];
+}
+
 void gemm_f64(tnad_ctx* c, char ta, char tb, int64_t M, int64_t N, int64_t K, double alpha, const double* A,
               int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc) {
   if (M <= 0 || N <= 0) return;
@@ -110,16 +169,39 @@ void gemm_f64(tnad_ctx* c, char ta, char tb, int64_t M, int64_t N, int64_t K, do
     return;
   }
   int ita = (ta == 'T' || ta == 't'), itb = (tb == 'T' || tb == 't');
-  const bool big = (M >= 64 && N >= 64);
+  if (N == 1 && (!ita || M <= kGemvMaxM)) {
+    // matrix-vector product: x = op(B) is a K-vector with stride ldb when tb = T
+    const int64_t incx = itb ? ldb : 1;
+    KernelTimer kt(c, "gemm_f64", 2.0 * (double)M * (double)K);
+    if (!ita) {
+      k_gemv_n<<<(int)std::min<int64_t>((M + 255) / 256, 4096), 256, 0, c->stream>>>(M, K, alpha, A, lda, B, incx,
+                                                                                     beta, C);
+      count_launch(c);
+    } else {
+      // K chunks of at least 2048 values, at most 2 CTAs per SM
+      const int64_t nch = std::max<int64_t>(1, std::min<int64_t>((K + 2047) / 2048, 2 * c->sm_count));
+      const int64_t kchunk = (K + nch - 1) / nch;
+      WsScope scope(c);
+      double* part = ws_d(c, nch * M);
+      k_gemv_t_part<<<(unsigned)nch, 256, 0, c->stream>>>(M, K, kchunk, A, lda, B, incx, part);
+      k_gemv_t_sum<<<1, kGemvMaxM, 0, c->stream>>>(M, (int)nch, part, alpha, beta, C);
+      count_launch(c, 2);
+    }
+    check_launch(c, "gemv_f64");
+    return;
+  }
+  // 64×64 tiles when they alone give half the SMs work, 32×32 otherwise
+  const int64_t tiles64 = ((M + 63) / 64) * ((N + 63) / 64);
+  const bool big = (M >= 64 && N >= 64 && tiles64 >= c->sm_count / 2);
   const int BM = big ? 64 : 32, BN = big ? 64 : 32;
   int64_t tiles = ((M + BM - 1) / BM) * ((N + BN - 1) / BN);
   // Each SM retires only ~2 DFMA per clock, so a GEMM whose output has fewer
   // tiles than SMs is split along K until about two CTAs per SM are busy
-  // (chunks of at least 64 K values; partial sums reduced in fixed order).
+  // (chunks of at least 16 K values; partial sums reduced in fixed order).
   int ks = 1;
-  if (tiles < 2 * c->sm_count && K >= 128) {
+  if (tiles < 2 * c->sm_count && K >= 32) {
     int64_t want = (2 * c->sm_count + tiles - 1) / tiles;
-    int64_t cap = K / 64;
+    int64_t cap = K / 16;
     ks = (int)std::max<int64_t>(1, std::min<int64_t>({want, cap, 128}));
   }
   int64_t kchunk = (K + ks - 1) / ks;

@@ -8,6 +8,7 @@
 // Singular values are the column norms, sorted descending by a rank kernel
 // (ties by index, so the result is deterministic).
 #include <algorithm>
+#include <atomic>
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
@@ -229,6 +230,180 @@ void jacobi_round_launch(tnad_ctx* c, T* W, T* V, int64_t m, int64_t n, int r, i
     k_jacobi_round_cta<16, T, EIG><<<np2, 128, 0, c->stream>>>(W, V, m, n, r, NP, tol, ae, fro2, flag);
 }
 
+// Block variant of the FP32 round.  The columns are grouped in blocks of 4
+// (the last one may be short) and the circle-method tournament runs over the
+// NB blocks (NB even; with an odd count of real blocks, block NB − 1 is a bye
+// whose columns lie beyond n and count as absent).  CTA k takes the block pair
+// (P, Q) of round r and holds their 8 columns of W (m rows) and V (n rows) in
+// shared memory.  It applies the same plane rotation as k_jacobi_round_cta to
+// every cross pair (column of P, column of Q): 4 inner rounds of 4 disjoint
+// pairs, TP threads per pair, each thread with 16 rows of the pair's columns in
+// registers (independent loads), the dot products reduced by shuffles and a
+// fixed-order sum of the pair's warp partials (every thread of the pair forms
+// the same angle).  In the first round of a sweep (intra = 1) the pairs inside
+// P and inside Q are rotated first (3 inner rounds), so that the NB − 1
+// launches of a sweep visit every column pair once, as the n − 1 launches of
+// the element rounds do, with a quarter of their launches and global passes.
+constexpr int kJB = 4;          // columns per block
+constexpr int kJBRows = 16;     // rows per thread
+template <bool EIG, int TP>
+__global__ void __launch_bounds__(kJB * TP) k_jacobi_block(float* __restrict__ W, float* __restrict__ V, int m, int n,
+                                                           int NB, int r, int intra, double tol, double abs_eps,
+                                                           const double* __restrict__ fro2,
+                                                           int* __restrict__ rotated) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  float* Ws = reinterpret_cast<float*>(smraw);  // 8 columns × m
+  float* Vs = Ws + (size_t)2 * kJB * m;         // 8 columns × n
+  __shared__ float red[kJB][TP / 32][3];
+  int P, Q;
+  pair_of(r, blockIdx.x, NB, &P, &Q);
+  const int tid = threadIdx.x, nt = blockDim.x;
+  auto gcol = [&](int c) { return c < kJB ? P * kJB + c : Q * kJB + (c - kJB); };
+  for (int c = 0; c < 2 * kJB; ++c) {
+    const int g = gcol(c);
+    if (g >= n) continue;
+    const float* wsrc = W + (int64_t)g * m;
+    const float* vsrc = V + (int64_t)g * n;
+    for (int i = tid; i < m; i += nt) Ws[(size_t)c * m + i] = wsrc[i];
+    for (int i = tid; i < n; i += nt) Vs[(size_t)c * n + i] = vsrc[i];
+  }
+  __syncthreads();
+  const float thr_abs = (float)abs_eps * sqrtf((float)fro2[0]);
+  const int slot = tid / TP, lt = tid % TP, wip = lt >> 5, lane = tid & 31;
+  int nrot = 0;
+  // one inner-round step for local columns (a, c) of this thread's pair; every
+  // thread of the CTA calls it once per inner round (the barrier inside)
+  auto process = [&](int a, int c) {
+    int ga = gcol(a), gc = gcol(c);
+    const bool present = ga < n && gc < n;
+    if (ga > gc) {
+      const int t = a;
+      a = c;
+      c = t;
+    }
+    float x[kJBRows], y[kJBRows], vx[kJBRows], vy[kJBRows];
+    float A = 0.f, B = 0.f, G = 0.f, G2 = 0.f;
+    if (present) {
+#pragma unroll
+      for (int e = 0; e < kJBRows; ++e) {
+        const int i = lt + TP * e;
+        x[e] = i < m ? Ws[(size_t)a * m + i] : 0.f;
+        y[e] = i < m ? Ws[(size_t)c * m + i] : 0.f;
+        vx[e] = i < n ? Vs[(size_t)a * n + i] : 0.f;
+        vy[e] = i < n ? Vs[(size_t)c * n + i] : 0.f;
+      }
+#pragma unroll
+      for (int e = 0; e < kJBRows; ++e) {
+        if (EIG) {
+          A = fmaf(vx[e], x[e], A);
+          B = fmaf(vy[e], y[e], B);
+          G = fmaf(vx[e], y[e], G);
+          G2 = fmaf(vy[e], x[e], G2);
+        } else {
+          A = fmaf(x[e], x[e], A);
+          B = fmaf(y[e], y[e], B);
+          G = fmaf(x[e], y[e], G);
+        }
+      }
+      if (EIG) G = 0.5f * (G + G2);
+      A = wsum_t(A);
+      B = wsum_t(B);
+      G = wsum_t(G);
+      if (lane == 0) {
+        red[slot][wip][0] = A;
+        red[slot][wip][1] = B;
+        red[slot][wip][2] = G;
+      }
+    }
+    __syncthreads();
+    bool do_rot = false;
+    float cs = 1.f, sn = 0.f;
+    if (present) {
+      A = B = G = 0.f;
+#pragma unroll
+      for (int w = 0; w < TP / 32; ++w) {
+        A += red[slot][w][0];
+        B += red[slot][w][1];
+        G += red[slot][w][2];
+      }
+      if (EIG) {
+        do_rot = G != 0.f && fabsf(G) > (float)tol * sqrtf(fabsf(A * B)) + thr_abs;
+      } else {
+        const float sa = sqrtf(A), sb = sqrtf(B);
+        do_rot = G != 0.f && A != 0.f && B != 0.f && fabsf(G) > (float)tol * sa * sb + thr_abs * (sa + sb);
+      }
+      if (do_rot) {
+        const float zeta = (B - A) / (2.f * G);
+        const float t =
+            fabsf(zeta) > 1e18f ? 0.5f / zeta : copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
+        cs = 1.f / sqrtf(1.f + t * t);
+        sn = cs * t;
+#pragma unroll
+        for (int e = 0; e < kJBRows; ++e) {
+          const int i = lt + TP * e;
+          if (i < m) {
+            Ws[(size_t)a * m + i] = cs * x[e] - sn * y[e];
+            Ws[(size_t)c * m + i] = sn * x[e] + cs * y[e];
+          }
+          if (i < n) {
+            Vs[(size_t)a * n + i] = cs * vx[e] - sn * vy[e];
+            Vs[(size_t)c * n + i] = sn * vx[e] + cs * vy[e];
+          }
+        }
+        if (lt == 0) ++nrot;
+      }
+    }
+    __syncthreads();
+  };
+  if (intra) {
+    // pairs inside P (slots 0, 1) and inside Q (slots 2, 3): 3 inner rounds
+    for (int ir = 0; ir < kJB - 1; ++ir) {
+      int a, c;
+      pair_of(ir, slot & 1, kJB, &a, &c);
+      if (slot >= 2) {
+        a += kJB;
+        c += kJB;
+      }
+      process(a, c);
+    }
+  }
+  // cross pairs: in inner round ir, slot k pairs P's column k with Q's column (k + ir) mod 4
+  for (int ir = 0; ir < kJB; ++ir) process(slot, kJB + ((slot + ir) & (kJB - 1)));
+  for (int c = 0; c < 2 * kJB; ++c) {
+    const int g = gcol(c);
+    if (g >= n) continue;
+    float* wdst = W + (int64_t)g * m;
+    float* vdst = V + (int64_t)g * n;
+    for (int i = tid; i < m; i += nt) wdst[i] = Ws[(size_t)c * m + i];
+    for (int i = tid; i < n; i += nt) vdst[i] = Vs[(size_t)c * n + i];
+  }
+  if (lt == 0 && nrot) atomicAdd(rotated, nrot);
+}
+
+// Threads per pair of the FP32 block rounds (16 rows each, 64 threads): 0 when
+// the block rounds do not apply (m beyond 1024 rows, or n > m).  Taller
+// matrices keep the element rounds: with 128 threads per pair the block rounds
+// were measured no faster at n = 1600, and their FP32 start needed more
+// refinement iterations there.
+inline int jacobi_block_tp(int64_t m, int64_t n) {
+  if (n > m || m > 64 * kJBRows) return 0;
+  return 64;
+}
+
+template <bool EIG>
+void jacobi_block_launch(tnad_ctx* c, float* W, float* V, int64_t m, int64_t n, int tp, int NB, int r, double tol,
+                         double ae, const double* fro2, int* flag) {
+  static std::atomic<bool> attr{false};
+  if (!attr) {
+    TNAD_CK(cudaFuncSetAttribute(k_jacobi_block<EIG, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+    attr = true;
+  }
+  (void)tp;  // 64 threads per pair (jacobi_block_tp)
+  const size_t sm = (size_t)2 * kJB * (m + n) * sizeof(float);
+  k_jacobi_block<EIG, 64><<<(unsigned)(NB / 2), kJB * 64, sm, c->stream>>>(W, V, (int)m, (int)n, NB, r,
+                                                                           r == 0 ? 1 : 0, tol, ae, fro2, flag);
+}
+
 // One Jacobi sweep (flag reset + the NP−1 rounds) recorded once as a CUDA
 // graph and replayed for every sweep: the rounds are short kernels whose
 // launch cost is comparable to their run time.  Very small matrices are
@@ -237,11 +412,18 @@ template <typename T, bool EIG = false>
 struct SweepGraph {
   cudaGraphExec_t exec = nullptr;
   double ae_ = -1.0;
+  int tp = 0;  // > 0 (FP32 only): block rounds (k_jacobi_block, tp threads per pair), NB − 1 launches a sweep
   ~SweepGraph() {
     if (exec) cudaGraphExecDestroy(exec);
   }
   void run(tnad_ctx* c, const char* family, T* W, T* V, int64_t m, int64_t n, int NP, double tol, double ae,
            const double* fro2, int* flag, double round_flops) {
+    if constexpr (sizeof(T) == 4) {
+      if (tp > 0) {
+        run_blocks(c, family, W, V, m, n, tol, ae, fro2, flag, round_flops * (double)(NP - 1));
+        return;
+      }
+    }
     if (NP < 64) {
       TNAD_CK(cudaMemsetAsync(flag, 0, sizeof(int), c->stream));
       for (int r = 0; r < NP - 1; ++r) {
@@ -274,6 +456,36 @@ struct SweepGraph {
       TNAD_CK(cudaGraphLaunch(exec, c->stream));
     }
     count_launch(c, NP - 1);
+    check_launch(c, family);
+  }
+  // one sweep of block rounds (NB − 1 launches of k_jacobi_block), captured
+  // once as a graph and replayed; sweep_flops: the sweep's algorithmic work
+  void run_blocks(tnad_ctx* c, const char* family, T* W, T* V, int64_t m, int64_t n, double tol, double ae,
+                  const double* fro2, int* flag, double sweep_flops) {
+    const int nreal = (int)((n + kJB - 1) / kJB);
+    const int NB = nreal + (nreal & 1);
+    if (exec && ae != ae_) {
+      TNAD_CK(cudaGraphExecDestroy(exec));
+      exec = nullptr;
+    }
+    if (!exec) {
+      cudaGraph_t g = nullptr;
+      TNAD_CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+      cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int), c->stream);
+      for (int r = 0; r < NB - 1 && e == cudaSuccess; ++r) {
+        jacobi_block_launch<EIG>(c, W, V, m, n, tp, NB, r, tol, ae, fro2, flag);
+        e = cudaGetLastError();
+      }
+      const cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+      if (e == cudaSuccess) e = e2;
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
+      if (g) cudaGraphDestroy(g);
+      if (e != cudaSuccess) fail(TNAD_ERR_CUDA, std::string("jacobi block sweep graph: ") + cudaGetErrorString(e));
+      ae_ = ae;
+    }
+    KernelTimer kt(c, family, sweep_flops, NB - 1);
+    TNAD_CK(cudaGraphLaunch(exec, c->stream));
+    count_launch(c, NB - 1);
     check_launch(c, family);
   }
 };
@@ -534,8 +746,10 @@ void svd_jacobi(tnad_ctx* c, const double* A, int64_t m, int64_t n, double* U, d
     // eigenvalue rule: rotate while |v_pᵀAv_q| > 2ε₃₂‖A‖_F (the FP32 floor);
     // SVD rule: relative orthogonality 4√m·ε₃₂ of the columns of W
     const double tol32 = refine ? 0.0 : 4.0 * std::sqrt((double)m) * FLT_EPSILON, ae32 = 2.0 * FLT_EPSILON;
+    // block rounds (b columns per block): 1/b of the launches and global passes
     SweepGraph<float> sweep32;
     SweepGraph<float, true> sweep32e;
+    if (c->jacobi_blocks) sweep32.tp = sweep32e.tp = jacobi_block_tp(m, n);
     const double round_flops = (double)(n / 2) * (12.0 * (double)m + 6.0 * (double)n);
     for (int sweep = 0; sweep < kMaxSweeps32; ++sweep) {
       if (refine)

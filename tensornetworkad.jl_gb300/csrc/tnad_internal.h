@@ -100,6 +100,9 @@ struct tnad_ctx {
   // and how often that refinement was taken / fell back to the sweeps
   bool eig_refine = true;
   int64_t eig_refined = 0, eig_fallback = 0;
+  // FP32 Jacobi sweeps of the symmetric SVD as block rounds (k_jacobi_block;
+  // false: one launch per element round, set by TNAD_JACOBI_BLOCKS=0)
+  bool jacobi_blocks = true;
   // kernel timer (tnad_ctx_kernel_timer): events around every launch of one
   // kernel family, with the algorithmic work (flops or bytes) of each launch
   std::string ktimer;
@@ -246,9 +249,6 @@ void svd_jacobi(tnad_ctx* c, const double* A, int64_t m, int64_t n, double* U, d
 // (column order of X).  fro2: ‖A‖²_F on the device.  false: no convergence
 // (X is then unusable and the caller falls back to Jacobi sweeps).
 bool eig_refine(tnad_ctx* c, const double* A, int64_t n, double* X, double* lam, const double* fro2);
-// The same refinement started from X = I for a small, nearly diagonal symmetric
-// p×p matrix; W, lam sorted by |λ| descending.  false: not converged.
-bool eigh_refine_small(tnad_ctx* c, const double* H, int64_t p, double* W, double* lam);
 // Symmetric eigendecomposition of a small p×p matrix (p ≤ 256) by cyclic Jacobi in
 // one CTA: A = W·diag(lam)·Wᵀ, sorted by |lam| descending.
 void eigh_small(tnad_ctx* c, const double* A, int64_t p, double* W, double* lam);

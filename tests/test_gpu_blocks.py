@@ -5,7 +5,9 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 SHAPES = [(1, 1, 1), (12, 12, 12), (33, 17, 5), (64, 64, 64), (130, 70, 300), (4, 4, 5000), (1024, 64, 64),
-          (256, 1024, 96)]
+          (256, 1024, 96),
+          # matrix-vector products (the Gram–Schmidt steps of GMRES) and small split-K products
+          (4000, 1, 31), (31, 1, 70000), (33, 1, 5000), (1, 1, 3000), (64, 64, 48), (96, 96, 40)]
 
 
 @pytest.mark.parametrize("M,N,K", SHAPES)

@@ -178,8 +178,10 @@ void gemm_f64(tnad_ctx* c, char ta, char tb, int64_t M, int64_t N, int64_t K, do
                                                                                      beta, C);
       count_launch(c);
     } else {
-      // K chunks of at least 2048 values, at most 2 CTAs per SM
-      const int64_t nch = std::max<int64_t>(1, std::min<int64_t>((K + 2047) / 2048, 2 * c->sm_count));
+      // K chunks of at least 512 values, at most 2 CTAs per SM: the FP64 pipe
+      // of every SM takes part (34 chunks of 2048 at K = 69632 left the
+      // product DFMA-bound on 34 SMs)
+      const int64_t nch = std::max<int64_t>(1, std::min<int64_t>((K + 511) / 512, 2 * c->sm_count));
       const int64_t kchunk = (K + nch - 1) / nch;
       WsScope scope(c);
       double* part = ws_d(c, nch * M);

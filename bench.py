@@ -172,6 +172,10 @@ FP64_NOMINAL_TFLOPS = 1.25  # GB300 FP64 (no measured FP64 figure exists for thi
 JACOBI_ROUND_TRAFFIC_BYTES = 16805888
 # GB300 FP32 (CUDA-core FMA) rate: 152 SMs × 128 FMA/clock × 2 flops × 2.07 GHz
 FP32_NOMINAL_TFLOPS = 80.5
+# dram__bytes_read.sum + dram__bytes_write.sum per launch of the FP64 tensor-core
+# GEMM (k_gemm_oz), mean over the first 300 of its launches in one cold D=4,
+# chi=64 solve (one ncu capture of that kernel on this workload)
+OZ_TRAFFIC_BYTES = 3321780
 
 
 def peaks():
@@ -418,7 +422,7 @@ def run_gb300(args):
                           "share_of_step": round(fms / 1e3 / t_dev, 4)}
     top = max(families, key=lambda k: families[k]["share_of_step"])
     roofline = dict(families[top], family=top,
-                    traffic=JACOBI_ROUND_TRAFFIC_BYTES if top == "jacobi_round" else None)
+                    traffic={"jacobi_round": JACOBI_ROUND_TRAFFIC_BYTES, "gemm_fp64tc": OZ_TRAFFIC_BYTES}.get(top))
     nA = int(np.asarray(sol.A).size)
     line = {
         "metric": metric_for(w),

@@ -15,6 +15,7 @@
 #include <cstdlib>
 #include <mutex>
 
+#include "tc_common.cuh"
 #include "tnad_internal.h"
 
 namespace tnad {
@@ -246,28 +247,70 @@ void jacobi_round_launch(tnad_ctx* c, T* W, T* V, int64_t m, int64_t n, int r, i
 // the element rounds do, with a quarter of their launches and global passes.
 constexpr int kJB = 4;          // columns per block
 constexpr int kJBRows = 16;     // rows per thread
+//
+// With `bulk` (m and n multiples of 4, W and V 16-byte aligned) the columns
+// move between global and shared memory as one-dimensional bulk copies
+// (cp.async.bulk): thread 0 issues the 16 loads against one mbarrier and,
+// at the end, the 16 stores; the wait on the mbarrier is bounded (2 s of
+// %globaltimer), after which the CTA sets *err, waits once more (bounded) for
+// its copies in flight and returns without rotating.
 template <bool EIG, int TP>
 __global__ void __launch_bounds__(kJB * TP) k_jacobi_block(float* __restrict__ W, float* __restrict__ V, int m, int n,
                                                            int NB, int r, int intra, double tol, double abs_eps,
                                                            const double* __restrict__ fro2,
-                                                           int* __restrict__ rotated) {
+                                                           int* __restrict__ rotated, int bulk, int* __restrict__ err) {
   extern __shared__ __align__(16) unsigned char smraw[];
   float* Ws = reinterpret_cast<float*>(smraw);  // 8 columns × m
   float* Vs = Ws + (size_t)2 * kJB * m;         // 8 columns × n
   __shared__ float red[kJB][TP / 32][3];
+  __shared__ __align__(8) uint64_t bar;
   int P, Q;
   pair_of(r, blockIdx.x, NB, &P, &Q);
   const int tid = threadIdx.x, nt = blockDim.x;
   auto gcol = [&](int c) { return c < kJB ? P * kJB + c : Q * kJB + (c - kJB); };
-  for (int c = 0; c < 2 * kJB; ++c) {
-    const int g = gcol(c);
-    if (g >= n) continue;
-    const float* wsrc = W + (int64_t)g * m;
-    const float* vsrc = V + (int64_t)g * n;
-    for (int i = tid; i < m; i += nt) Ws[(size_t)c * m + i] = wsrc[i];
-    for (int i = tid; i < n; i += nt) Vs[(size_t)c * n + i] = vsrc[i];
+  if (bulk) {
+    const uint32_t b = tc::su32(&bar);
+    if (tid == 0) {
+      tc::mbar_init(b, 1);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (tid == 0) {
+      uint32_t bytes = 0;
+      for (int c = 0; c < 2 * kJB; ++c)
+        if (gcol(c) < n) bytes += (uint32_t)(m + n) * 4u;
+      tc::mbar_expect_tx(b, bytes);
+      for (int c = 0; c < 2 * kJB; ++c) {
+        const int g = gcol(c);
+        if (g >= n) continue;
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                tc::su32(Ws + (size_t)c * m)),
+            "l"(W + (int64_t)g * m), "r"(m * 4), "r"(b)
+            : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                tc::su32(Vs + (size_t)c * n)),
+            "l"(V + (int64_t)g * n), "r"(n * 4), "r"(b)
+            : "memory");
+      }
+    }
+    const bool ok = tc::mbar_wait(b, 0, err, 1, 2000000000ull);
+    if (__syncthreads_or(ok ? 0 : 1)) {
+      tc::mbar_wait(b, 0, err, 1, 2000000000ull);  // the copies still in flight, bounded
+      return;
+    }
+  } else {
+    for (int c = 0; c < 2 * kJB; ++c) {
+      const int g = gcol(c);
+      if (g >= n) continue;
+      const float* wsrc = W + (int64_t)g * m;
+      const float* vsrc = V + (int64_t)g * n;
+      for (int i = tid; i < m; i += nt) Ws[(size_t)c * m + i] = wsrc[i];
+      for (int i = tid; i < n; i += nt) Vs[(size_t)c * n + i] = vsrc[i];
+    }
+    __syncthreads();
   }
-  __syncthreads();
   const float thr_abs = (float)abs_eps * sqrtf((float)fro2[0]);
   const int slot = tid / TP, lt = tid % TP, wip = lt >> 5, lane = tid & 31;
   int nrot = 0;
@@ -369,13 +412,34 @@ __global__ void __launch_bounds__(kJB * TP) k_jacobi_block(float* __restrict__ W
   }
   // cross pairs: in inner round ir, slot k pairs P's column k with Q's column (k + ir) mod 4
   for (int ir = 0; ir < kJB; ++ir) process(slot, kJB + ((slot + ir) & (kJB - 1)));
-  for (int c = 0; c < 2 * kJB; ++c) {
-    const int g = gcol(c);
-    if (g >= n) continue;
-    float* wdst = W + (int64_t)g * m;
-    float* vdst = V + (int64_t)g * n;
-    for (int i = tid; i < m; i += nt) wdst[i] = Ws[(size_t)c * m + i];
-    for (int i = tid; i < n; i += nt) vdst[i] = Vs[(size_t)c * n + i];
+  if (bulk) {
+    // the rotations wrote shared memory through the generic proxy: fence it
+    // towards the async proxy before the bulk stores read it
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      for (int c = 0; c < 2 * kJB; ++c) {
+        const int g = gcol(c);
+        if (g >= n) continue;
+        asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(W + (int64_t)g * m),
+                     "r"(tc::su32(Ws + (size_t)c * m)), "r"(m * 4)
+                     : "memory");
+        asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(V + (int64_t)g * n),
+                     "r"(tc::su32(Vs + (size_t)c * n)), "r"(n * 4)
+                     : "memory");
+      }
+      asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+      asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    }
+  } else {
+    for (int c = 0; c < 2 * kJB; ++c) {
+      const int g = gcol(c);
+      if (g >= n) continue;
+      float* wdst = W + (int64_t)g * m;
+      float* vdst = V + (int64_t)g * n;
+      for (int i = tid; i < m; i += nt) wdst[i] = Ws[(size_t)c * m + i];
+      for (int i = tid; i < n; i += nt) vdst[i] = Vs[(size_t)c * n + i];
+    }
   }
   if (lt == 0 && nrot) atomicAdd(rotated, nrot);
 }
@@ -400,8 +464,11 @@ void jacobi_block_launch(tnad_ctx* c, float* W, float* V, int64_t m, int64_t n, 
   }
   (void)tp;  // 64 threads per pair (jacobi_block_tp)
   const size_t sm = (size_t)2 * kJB * (m + n) * sizeof(float);
+  // bulk copies need 16-byte aligned columns: m, n multiples of 4 and aligned bases
+  const int bulk = (m % 4 == 0 && n % 4 == 0 && ((uintptr_t)W & 15) == 0 && ((uintptr_t)V & 15) == 0) ? 1 : 0;
   k_jacobi_block<EIG, 64><<<(unsigned)(NB / 2), kJB * 64, sm, c->stream>>>(W, V, (int)m, (int)n, NB, r,
-                                                                           r == 0 ? 1 : 0, tol, ae, fro2, flag);
+                                                                           r == 0 ? 1 : 0, tol, ae, fro2, flag, bulk,
+                                                                           flag + 2);
 }
 
 // One Jacobi sweep (flag reset + the NP−1 rounds) recorded once as a CUDA
@@ -756,8 +823,13 @@ void svd_jacobi(tnad_ctx* c, const double* A, int64_t m, int64_t n, double* U, d
         sweep32e.run(c, "jacobi_round_f32", W32, V32, m, n, NP, tol32, ae32, fro2, flag, round_flops);
       else
         sweep32.run(c, "jacobi_round_f32", W32, V32, m, n, NP, tol32, ae32, fro2, flag, round_flops);
-      TNAD_CK(cudaMemcpyAsync(c->h_flag, flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+      // rotation count, and the error slot of the block rounds' bounded waits
+      TNAD_CK(cudaMemcpyAsync(c->h_flag, flag, 3 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
       TNAD_CK(cudaStreamSynchronize(c->stream));
+      if (c->h_flag[2] != 0) {
+        TNAD_CK(cudaMemsetAsync(flag + 2, 0, sizeof(int), c->stream));
+        fail(TNAD_ERR_TIMEOUT, "jacobi block round: bounded mbarrier wait expired");
+      }
       if (trace) std::fprintf(stderr, "[tnad trace] svd n=%lld fp32 sweep %d rotations %d\n", (long long)n, sweep, c->h_flag[0]);
       // The FP64 polish re-converges the small-σ columns anyway (V32's absolute
       // FP32 error is large relative to them), so the FP32 phase stops once

@@ -195,6 +195,9 @@ __global__ void k_eig_from_svd(const double* __restrict__ U, const double* __res
 // solver).  By then Q carries the previous Ritz basis, so H is nearly diagonal
 // and a few sweeps suffice; λ_i = σ_i·sign(u_i·v_i), ordered by |λ| descending.
 void eigh_small_fp64(tnad_ctx* c, const double* H, int64_t p, double* W, double* lam) {
+  // the one-CTA FP32 solve polished by matrix products; the FP64 Jacobi SVD
+  // below remains the fallback
+  if (eigh_fp32_refined(c, H, p, W, lam)) return;
   WsScope scope(c);
   double* Up = ws_d(c, p * p);
   double* Sp = ws_d(c, p);

@@ -478,6 +478,33 @@ __global__ void k_ref_coldots(const double* __restrict__ X, const double* __rest
 
 int nblk(int64_t n, int t = 256) { return (int)std::min<int64_t>((n + t - 1) / t, 4096); }
 
+// W[:, r] = X[:, j], lam_out[r] = lam[j] with r the rank of |λ_j| (descending,
+// ties by index); one CTA of 256 threads per column j
+__global__ void __launch_bounds__(256) k_ref_sort_abs(const double* __restrict__ X, const double* __restrict__ lam,
+                                                      int n, double* __restrict__ W, double* __restrict__ lam_out) {
+  const int j = blockIdx.x;
+  __shared__ int part[8];
+  __shared__ int rank_sh;
+  const double a = fabs(lam[j]);
+  int r = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double b = fabs(lam[i]);
+    r += (b > a || (b == a && i < j)) ? 1 : 0;
+  }
+  for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = r;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int w = 0; w < 8; ++w) t += part[w];
+    rank_sh = t;
+    lam_out[t] = lam[j];
+  }
+  __syncthreads();
+  const int64_t rr = rank_sh;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) W[i + rr * n] = X[i + (int64_t)j * n];
+}
+
 }  // namespace
 
 bool eig_refine(tnad_ctx* c, const double* A, int64_t n64, double* X, double* lam, const double* fro2) {
@@ -574,6 +601,29 @@ bool eig_refine(tnad_ctx* c, const double* A, int64_t n64, double* X, double* la
   k_ref_coldots<<<nblk(col_threads), 256, 0, c->stream>>>(X, AX, n, lam);
   count_launch(c);
   check_launch(c, "eig_refine_lam");
+  return true;
+}
+
+// Eigendecomposition H = W·diag(lam)·Wᵀ of a small symmetric p×p matrix
+// (p ≤ 256) to FP64 accuracy: the one-CTA FP32 Jacobi solve (eigenvalue rule,
+// so ±λ pairs stay apart) polished by the product refinement above, sorted by
+// |λ| descending.  false: the refinement did not converge (W, lam untouched).
+bool eigh_fp32_refined(tnad_ctx* c, const double* H, int64_t p, double* W, double* lam) {
+  if (!c->eig_refine || p < 2 || p > 256) return false;
+  WsScope scope(c);
+  double* X = ws_d(c, p * p);
+  double* l = ws_d(c, p);
+  double* fro2 = ws_d(c, 1);
+  eigh_small_prec(c, true, H, p, X, l, 40, nullptr);
+  sumsq_dev(c, H, p * p, fro2);
+  if (!eig_refine(c, H, p, X, l, fro2)) {
+    ++c->eig_fallback;
+    return false;
+  }
+  ++c->eig_refined;
+  k_ref_sort_abs<<<(unsigned)p, 256, 0, c->stream>>>(X, l, (int)p, W, lam);
+  count_launch(c);
+  check_launch(c, "eigh_fp32_refined");
   return true;
 }
 

@@ -249,6 +249,10 @@ void svd_jacobi(tnad_ctx* c, const double* A, int64_t m, int64_t n, double* U, d
 // (column order of X).  fro2: ‖A‖²_F on the device.  false: no convergence
 // (X is then unusable and the caller falls back to Jacobi sweeps).
 bool eig_refine(tnad_ctx* c, const double* A, int64_t n, double* X, double* lam, const double* fro2);
+// FP64-accurate eigendecomposition of a small symmetric p×p matrix (p ≤ 256):
+// one-CTA FP32 Jacobi, then eig_refine; W, lam sorted by |λ| descending.
+// false: the refinement did not converge (W, lam untouched).
+bool eigh_fp32_refined(tnad_ctx* c, const double* H, int64_t p, double* W, double* lam);
 // Symmetric eigendecomposition of a small p×p matrix (p ≤ 256) by cyclic Jacobi in
 // one CTA: A = W·diag(lam)·Wᵀ, sorted by |lam| descending.
 void eigh_small(tnad_ctx* c, const double* A, int64_t p, double* W, double* lam);

@@ -54,8 +54,11 @@ def ein(spec: str, *ops):
 
 
 def as_t(x) -> torch.Tensor:
+    """FP64 tensor, or complex128 for complex input (ComplexF64 in the reference)."""
     if isinstance(x, torch.Tensor):
-        return x.to(DT)
+        return x if x.is_complex() else x.to(DT)
+    if np.iscomplexobj(x):
+        return torch.as_tensor(np.asarray(x, dtype=np.complex128))
     return torch.as_tensor(np.asarray(x, dtype=np.float64))
 
 
@@ -226,7 +229,7 @@ def trg_svd(t, dmax, tol):
     FS = s[:dmax]
     sq = torch.sqrt(FS)
     uu = reshape_f(u[:, :dmax] * sq[None, :], (d1, d2, dmax))
-    vv = reshape_f(v.T[:dmax, :] * sq[:, None], (dmax, d3, d4))
+    vv = reshape_f(v.conj().T[:dmax, :] * sq[:, None], (dmax, d3, d4))  # copy(v')[1:dmax, :]
     return uu, vv
 
 
@@ -289,8 +292,8 @@ def init_random(D: int, chi: int, rng: np.random.Generator):
     """_initializect_square(bulk, Val(:random), χ)  src/ctmrg.jl:66-72 (NumPy RNG)."""
     corner = torch.as_tensor(rng.standard_normal((chi, chi)))
     edge = torch.as_tensor(rng.standard_normal((chi, D, chi)))
-    corner = corner + corner.T
-    edge = edge + edge.permute(2, 1, 0)
+    corner = corner + corner.conj().T
+    edge = edge + edge.conj().permute(2, 1, 0)
     return corner, edge
 
 
@@ -302,9 +305,9 @@ def enlarged_corner(bulk, corner, edge):
 
 
 def project_edge(bulk, edge, z):
-    """ein"abjcd,abi,dck -> ijk"(tp, z, z) with tp = ein"iam,jkla -> ijklm"(edge, bulk)
+    """ein"abjcd,abi,dck -> ijk"(tp, conj(z), z) with tp = ein"iam,jkla -> ijklm"(edge, bulk)
     (src/ctmrg.jl:131,140), contracted without materialising tp."""
-    y1 = ein("aed,abi->edbi", edge, z)
+    y1 = ein("aed,abi->edbi", edge, z.conj())
     y2 = ein("edbi,bjce->dijc", y1, bulk)
     return ein("dijc,dck->ijk", y2, z)
 
@@ -314,15 +317,15 @@ def ctmrgstep(bulk, corner, edge):
     D, chi = bulk.shape[0], corner.shape[0]
     cp = enlarged_corner(bulk, corner, edge)
     cpmat = reshape_f(cp, (chi * D, chi * D))
-    cpmat = cpmat + cpmat.T
+    cpmat = cpmat + cpmat.conj().T                      # cpmat += adjoint(cpmat)
     u, s, v = svd(cpmat)
     z = reshape_f(u[:, :chi], (chi, D, chi))
-    w = ein("abcd,abi->icd", cp, z)
+    w = ein("abcd,abi->icd", cp, z.conj())               # ein"abcd,abi,cdj -> ij"(cp, conj(z), z)
     corner_n = ein("icd,cdj->ij", w, z)
     edge_n = project_edge(bulk, edge, z)
     vals = (s / s[0]).detach()
-    corner_n = corner_n + corner_n.T
-    edge_n = edge_n + edge_n.permute(2, 1, 0)
+    corner_n = corner_n + corner_n.conj().T              # corner += corner'
+    edge_n = edge_n + edge_n.conj().permute(2, 1, 0)     # edge += ein"ijk -> kji"(conj(edge))
     corner_n = corner_n / norm(corner_n)
     edge_n = edge_n / norm(edge_n)
     return corner_n, edge_n, vals
@@ -369,10 +372,10 @@ def indexperm_symmetrize(x: torch.Tensor) -> torch.Tensor:
 
 
 def double_layer(A: torch.Tensor):
-    """ap and a of src/variationalipeps.jl:32-34 (real A: conj(A) = A)."""
+    """ap and a of src/variationalipeps.jl:32-34."""
     d, s = A.shape[0], A.shape[4]
     D = d * d
-    ap = ein("abcdx,ijkly->aibjckdlxy", A, A)
+    ap = ein("abcdx,ijkly->aibjckdlxy", A, A.conj())
     ap = reshape_f(ap, (D, D, D, D, s, s))
     a = ein("ijklaa->ijkl", ap)
     return ap, a
@@ -408,6 +411,8 @@ def energy_and_grad(h, bulk, chi: int, tol: float, maxit: int):
     """(E, dE/dbulk, steps): Zygote.gradient(x -> energy(h, IPEPS(x); ...), bulk)."""
     x = as_t(bulk).clone().requires_grad_(True)
     e, steps = energy(h, x, chi, tol, maxit, return_steps=True)
+    if e.is_complex():  # Zygote.gradient(x -> real(energy(...)), bulk): ∂/∂Re + i ∂/∂Im
+        e = e.real
     (g,) = torch.autograd.grad(e, x)
     return float(e.detach()), g.numpy(), steps
 
@@ -417,14 +422,23 @@ def optimiseipeps(bulk, h, chi: int, tol: float, maxit: int, f_tol: float = 1e-6
     import scipy.optimize
 
     shape = np.asarray(bulk).shape
+    cplx = np.iscomplexobj(bulk)
+    size = int(np.prod(shape))
+
+    def unpack(x):
+        return x[:size].reshape(shape) + 1j * x[size:].reshape(shape) if cplx else x.reshape(shape)
 
     def fg(x):
-        e, g, _ = energy_and_grad(h, x.reshape(shape), chi, tol, maxit)
-        return e, g.ravel()
+        # a complex tensor is optimised over (Re, Im); Zygote's gradient of a real
+        # function of a complex array is ∂/∂Re + i ∂/∂Im
+        e, g, _ = energy_and_grad(h, unpack(x), chi, tol, maxit)
+        return e, (np.concatenate([g.real.ravel(), g.imag.ravel()]) if cplx else g.ravel())
 
-    r = scipy.optimize.minimize(fg, np.asarray(bulk, dtype=np.float64).ravel(), jac=True, method="L-BFGS-B",
+    b = np.asarray(bulk)
+    x0 = np.concatenate([b.real.ravel(), b.imag.ravel()]) if cplx else np.asarray(b, dtype=np.float64).ravel()
+    r = scipy.optimize.minimize(fg, x0, jac=True, method="L-BFGS-B",
                                 options=dict(maxcor=m, maxiter=iters, ftol=f_tol, gtol=1e-10))
-    return float(r.fun), r.x.reshape(shape)
+    return float(r.fun), unpack(r.x)
 
 
 def magnetisation(beta: float, chi: int, rng: np.random.Generator, tol=1e-6, maxit=100):

@@ -6,7 +6,8 @@ module, and only as the checker or as the timed CPU restatement of the
 reference.  The product (``libtnad`` and the Python host mirror) never calls it.
 
 This is a line-by-line FP64 restatement of the Julia reference (which cannot run
-here: Julia, OMEinsum, Zygote and Optim are absent).  Every array keeps the
+here: Julia, OMEinsum, Zygote and Optim are absent), in ComplexF64 where the
+input is complex, with the reference's conjugations.  Every array keeps the
 reference's index order and every reshape is column-major (``reshape_f``), as in
 Julia.  Gradients come from torch autograd, which reproduces Zygote's generic
 adjoints (einsum, permutedims, reshape, maximum, log); the two custom adjoints

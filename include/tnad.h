@@ -163,7 +163,8 @@ int tnad_svd(tnad_ctx* ctx, const double* A, int m, int n, double* U, double* S,
    U = V·sign(λ).  For n ≥ 256 FP32 Jacobi sweeps are polished to FP64 accuracy
    by a refinement made of matrix products (FP64 Jacobi sweeps where that does
    not converge); prec = TNAD_PREC_FP64 runs those products as DFMA tiles,
-   TNAD_PREC_FP64_TC on the tensor cores.  Host pointers. */
+   TNAD_PREC_FP64_TC on the tensor cores (TNAD_ERR_STATE without tcgen05).
+   Host pointers. */
 int tnad_svd_sym(tnad_ctx* ctx, int prec, const double* A, int n, double* U, double* S, double* V);
 /* Diagnostics of the symmetric SVDs run on this context (no reference
    counterpart): how many took the product refinement and how many fell back

@@ -210,6 +210,8 @@ extern "C" int tnad_svd_sym(tnad_ctx* c, int prec, const double* A, int n, doubl
   TNAD_REQUIRE(A && U && S && V && n >= 1, TNAD_ERR_ARG, "tnad_svd_sym: needs n >= 1 and non-null arrays");
   TNAD_REQUIRE(prec == TNAD_PREC_FP64 || prec == TNAD_PREC_FP64_TC, TNAD_ERR_ARG,
                "tnad_svd_sym: prec must be TNAD_PREC_FP64 or TNAD_PREC_FP64_TC");
+  TNAD_REQUIRE(prec != TNAD_PREC_FP64_TC || c->tc_ok, TNAD_ERR_STATE,
+               "tnad_svd_sym: TNAD_PREC_FP64_TC needs an sm_100-family GPU (tcgen05)");
   Fp64TcScope route(c, prec == TNAD_PREC_FP64_TC);
   WsScope scope(c);
   const int64_t nn = (int64_t)n * n;

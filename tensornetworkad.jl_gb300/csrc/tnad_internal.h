@@ -100,6 +100,10 @@ struct tnad_ctx {
   // and how often that refinement was taken / fell back to the sweeps
   bool eig_refine = true;
   int64_t eig_refined = 0, eig_fallback = 0;
+  // size n whose last refinement fell back, and how many more SVDs of that
+  // size go straight to the FP64 sweeps (jacobi.cu, kEigSkip)
+  int64_t eig_skip_n = 0;
+  int eig_skip_left = 0;
   // FP32 Jacobi sweeps of the symmetric SVD as block rounds (k_jacobi_block;
   // false: one launch per element round, set by TNAD_JACOBI_BLOCKS=0)
   bool jacobi_blocks = true;
